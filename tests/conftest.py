@@ -1,0 +1,25 @@
+"""Shared test configuration.
+
+Tests marked ``gpu`` need a CUDA device and the built libvfps; everything
+else runs on the CPU (oracle checks, host logic, C-ABI symbol checks).
+"""
+import json
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+@pytest.fixture(scope="session")
+def golden():
+    with open(os.path.join(ROOT, "tests", "golden",
+                           "reference_tests.json")) as f:
+        return json.load(f)
