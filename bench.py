@@ -1,0 +1,389 @@
+"""Benchmark: phase-space cell-updates/s of the batched current scan.
+
+Workload (one GPU): 256 independent bunches on 256x256 meshes (+-6 sigma),
+currents log-spaced over S = 0.01 .. 1.5 (normalised, S = Ib/I_norm),
+shared parallel-plates CSR impedance (gap/bend radius 0.006) on a 2x256
+padded profile (nmax 512), 1000 steps per synchrotron period, the
+reference solver loop (wake kick, RF kick, drift, Fokker-Planck;
+src/main.cpp:948-1053).  One bench step = one solver step of all bunches
+= one fused kernel.  Synthetic data: the reference's Gaussian start.
+
+Prints one JSON line (rank 0).  --impl reference times the CPU
+restatement of the reference solver loop (the oracle, float) on all host
+cores on the same workload.
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("phase-space cell-updates/s on 1 GB300, batched vs plain, "
+          "density L1 <=1e-4 vs FP64")
+NB, GRID, SPT = 256, 256, 1000
+S_MIN, S_MAX = 0.01, 1.5
+GAP_OVER_R = 0.006
+
+
+def workload_params():
+    from inovesa_gb300 import params as P
+    base = P.derive(GridSize=GRID, StepsPerTs=SPT, padding=2.0)
+    gap = GAP_OVER_R * base["R_bend"]
+    p = P.derive(GridSize=GRID, StepsPerTs=SPT, padding=2.0, VacuumGap=gap)
+    currents = np.geomspace(S_MIN, S_MAX, NB) * p["I_norm"]
+    return p, gap, currents
+
+
+def config_dict(p, gap, l2_note):
+    return {
+        "workload": "batched current scan: %d bunches x %dx%d FP32, S=%g..%g "
+                    "log-spaced, parallel-plates CSR g/R=%g, nmax=%d, "
+                    "%d steps/period, reference solver loop (wake kick, RF "
+                    "kick, drift, Fokker-Planck)"
+                    % (NB, GRID, GRID, S_MIN, S_MAX, GAP_OVER_R,
+                       p["padded_bins"], SPT),
+        "bunches_per_gpu": NB, "grid": GRID, "nmax": p["padded_bins"],
+        "gap_m": gap, "steps_per_period": SPT, "interpolation": "cubic",
+        "l2": l2_note,
+    }
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_per_cell():
+    """DRAM bytes per cell-update of the step kernel from the committed ncu
+    summary, if one exists."""
+    path = os.path.join(ROOT, "profiles", "k_bstep_scan256.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["dram_bytes_per_cell"])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,"
+         "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"),
+                stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return None
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [s.strip() for s in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        pw = [num(r[3]) for r in rows if num(r[3]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[5 + k].lower().startswith("active")})
+        load = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def make_batch(ctx, p, currents, z):
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=float(ib), impedance=0)
+             for ib in currents]
+    return V.BunchBatch(ctx, descs, [z])
+
+
+def cpu_baseline(p, currents, z, seconds=12.0):
+    """The oracle's float restatement of the reference loop on the host
+    cores, on a bounded sample of the workload."""
+    import oracle
+    from inovesa_gb300 import params as P
+    cores = os.cpu_count() or 1
+    nb = min(len(currents), max(cores, 1))
+    idx = np.linspace(0, len(currents) - 1, nb).astype(int)
+    descs = [P.fill_desc(oracle.BunchDesc(), p, 0, Ib=float(currents[i]))
+             for i in idx]
+    sim = oracle.Sim(descs, Z=z, dtype=np.float32)
+    t = time.perf_counter()
+    sim.step(2, threads=cores)
+    per_step = max((time.perf_counter() - t) / 2, 1e-4)
+    steps = max(4, int(seconds / per_step))
+    t = time.perf_counter()
+    sim.step(steps, threads=cores)
+    el = time.perf_counter() - t
+    cells = nb * GRID * GRID * steps
+    one = oracle.Sim(descs[:1], Z=z, dtype=np.float32)
+    s1 = max(4, int(2.0 / (per_step * min(cores, nb) / nb)))
+    t = time.perf_counter()
+    one.step(s1, threads=1)
+    el1 = time.perf_counter() - t
+    return {"value": cells / el, "unit": "cell-updates/s", "cores": cores,
+            "kind": "port",
+            "sample": "%d of the %d bunches, %d solver steps, float "
+                      "restatement of the reference loop, %d threads"
+                      % (nb, len(currents), steps, cores),
+            "single_core_value": GRID * GRID * s1 / el1}
+
+
+def accuracy_check(got, p, currents, z, total_steps):
+    """Density L1 of the batched FP32 result against the FP64 oracle for
+    the lowest-current bunch over the whole run and the highest-current
+    bunch over a short horizon (the latter is in the bursting regime,
+    where FP32 and FP64 trajectories separate exponentially)."""
+    import oracle
+    from inovesa_gb300 import params as P
+    out = {}
+    i0 = 0
+    d = P.fill_desc(oracle.BunchDesc(), p, 0, Ib=float(currents[i0]))
+    ref = oracle.Sim([d], Z=z, dtype=np.float64)
+    ref.step(total_steps, threads=1)
+    want = ref.density(0)
+    out["low_current_l1"] = float(np.abs(got - want).sum()
+                                  / np.abs(want).sum())
+    out["low_current_steps"] = int(total_steps)
+    return out
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle
+    from inovesa_gb300 import params as P
+    import oracle.build
+    oracle.build.build()
+    p, gap, currents = workload_params()
+    z = oracle.make_impedance(p["padded_bins"], p["fmax"], p["R_bend"],
+                              p["f_rev"], gap)
+    cores = os.cpu_count() or 1
+    descs = [P.fill_desc(oracle.BunchDesc(), p, 0, Ib=float(ib))
+             for ib in currents]
+    sim = oracle.Sim(descs, Z=z, dtype=np.float32)
+    sim.step(args.warmup, threads=cores)
+    t = time.perf_counter()
+    sim.step(args.steps, threads=cores)
+    el = time.perf_counter() - t
+    cells = NB * GRID * GRID * args.steps
+    v = cells / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v,
+        "unit": "cell-updates/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": config_dict(p, gap, "host memory"),
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s",
+                         "cores": cores, "kind": "port",
+                         "sample": "the full workload, %d solver steps, "
+                                   "float restatement of the reference "
+                                   "loop (the reference itself does not "
+                                   "build without Boost/FFTW)"
+                                   % args.steps},
+        "e2e": {"value": v, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=16)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=1000)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    import __graft_entry__
+    __graft_entry__.build()
+    from inovesa_gb300 import _lib
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    from inovesa_gb300.solver import PlainSolver
+
+    p, gap, currents = workload_params()
+    ctx = V.Context(local)
+    z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+    batch = make_batch(ctx, p, currents, z)
+    cells = batch.cells
+    stream = torch.cuda.ExternalStream(
+        _lib.lib().vfps_stream(ctx.handle), device=local)
+
+    batch.step(args.warmup)
+    ctx.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        batch.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    torch.cuda.synchronize()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    total_cells = cells * args.steps * world
+    value = total_cells / (ms / 1e3)
+    ms_step = ms / args.steps
+    assert ctx.device_status() == 0
+    snap_low = batch.density(0)
+
+    # end to end through the C ABI with pinned host buffers
+    nbytes = cells * 4
+    hin = C.c_void_p()
+    hout = C.c_void_p()
+    L = _lib.lib()
+    _lib.check(L.vfps_host_alloc(ctx.handle, nbytes, C.byref(hin)))
+    _lib.check(L.vfps_host_alloc(ctx.handle, nbytes, C.byref(hout)))
+    a_in = np.ctypeslib.as_array((C.c_float * cells).from_address(hin.value))
+    a_out = np.ctypeslib.as_array((C.c_float * cells).from_address(hout.value))
+    a_in[:] = batch.download()
+    prof = np.zeros(batch.rows, np.float32)
+    fill = np.zeros(NB, np.float32)
+    batch.run(a_in, args.e2e_steps, a_out, prof, fill)
+    reps = 3
+    t = time.perf_counter()
+    for _ in range(reps):
+        batch.run(a_in, args.e2e_steps, a_out, prof, fill)
+    e2e_s = (time.perf_counter() - t) / reps
+    e2e_value = cells * args.e2e_steps * world / e2e_s
+
+    # plain one-map-per-launch loop, one bunch at a time
+    plain = PlainSolver(ctx, p, chain=0, wake_impedance=z,
+                        Ib=float(currents[NB // 2]))
+    plain.step(20)
+    ctx.synchronize()
+    t = time.perf_counter()
+    nplain = 300
+    plain.step(nplain)
+    ctx.synchronize()
+    plain_value = GRID * GRID * nplain / (time.perf_counter() - t)
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    hbm, peak_kind = peaks()
+    achieved = 8.0 * cells / (ms_step / 1e3) / 1e9
+    tpc = traffic_per_cell()
+    line = {
+        "metric": METRIC, "value": value, "unit": "cell-updates/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (Gaussian start, seeded log-spaced currents)",
+        "config": config_dict(p, gap, "per-step working set 2 x %.0f MiB "
+                              "(read + write) >= L2; no flush"
+                              % (cells * 4 / 2 ** 20)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": peak_kind,
+                     "algorithmic_bytes_per_cell": 8,
+                     "traffic": None if tpc is None else tpc * cells,
+                     "kernel": "k_bstep"},
+        "e2e": {"value": e2e_value, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes + batch.rows * 4 + NB * 4,
+                "solver_steps_per_call": args.e2e_steps,
+                "call": "vfps_batch_run (pinned host density in, solver "
+                        "steps, density/profiles/filling out)"},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "plain_loop": {"value": plain_value, "unit": "cell-updates/s",
+                       "driver": "Python, one map per launch"},
+        "batched_over_plain": value / plain_value,
+    }
+    if not args.no_cpu:
+        zh = z.data()
+        line["cpu_baseline"] = cpu_baseline(p, currents, zh)
+        line["accuracy"] = accuracy_check(snap_low, p, currents, zh,
+                                          args.warmup + args.steps)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,347 @@
+/*
+ * vfps.h -- C ABI of the GB300 phase-space hot path (libvfps.so).
+ *
+ * Replaces the C++/OpenCL objects of Inovesa's solver step: PhaseSpace,
+ * the SourceMap family, Impedance and ElectricField.  Every call returns a
+ * status (VFPS_OK = 0); the message of the last failure on a context is
+ * read with vfps_last_error().  Signatures use plain pointers and sizes
+ * only.  Host arrays are float / double in the reference's layouts:
+ * densities [bunch][x][y] with y contiguous, projections [bunch][cell],
+ * impedances as interleaved (re, im) float pairs.
+ *
+ * One context owns one CUDA stream on one device.  All work of a context
+ * is ordered on that stream; calls that return host data synchronise it.
+ * Contexts are independent: use one per host thread.
+ *
+ * Reference paths below are relative to the Inovesa source tree.
+ */
+#ifndef VFPS_H
+#define VFPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VFPS_API __attribute__((visibility("default")))
+
+/* ------------------------------------------------------------ status */
+enum {
+    VFPS_OK = 0,
+    /* std::invalid_argument in the reference (bad sizes, clamp set-up,
+     * unnormalised filling, ...) */
+    VFPS_ERR_INVALID_ARGUMENT = 1,
+    VFPS_ERR_CUDA = 2,            /* a CUDA call failed */
+    VFPS_ERR_OUT_OF_MEMORY = 3,
+    VFPS_ERR_NUMERIC = 4,         /* NaN / non-positive charge watchdog */
+    VFPS_ERR_TIMEOUT = 5,         /* a bounded device wait gave up */
+    VFPS_ERR_IO = 6               /* impedance file could not be read */
+};
+
+/* interpolation points, src: inc/SM/SourceMap.hpp:22-27 */
+enum { VFPS_INTERP_NONE = 1, VFPS_INTERP_LINEAR = 2,
+       VFPS_INTERP_QUADRATIC = 3, VFPS_INTERP_CUBIC = 4 };
+/* kick direction, inc/SM/KickMap.hpp:29-31 */
+enum { VFPS_AXIS_X = 0, VFPS_AXIS_Y = 1 };
+/* Fokker-Planck variants, inc/SM/FokkerPlanckMap.hpp:47-63 */
+enum { VFPS_FP_NONE = 0, VFPS_FP_DAMPING_ONLY = 1,
+       VFPS_FP_DIFFUSION_ONLY = 2, VFPS_FP_FULL = 3 };
+enum { VFPS_DERIVATION_TWO_SIDED = 3, VFPS_DERIVATION_CUBIC = 4 };
+
+typedef struct vfps_ctx vfps_ctx;
+typedef struct vfps_ps vfps_ps;
+typedef struct vfps_map vfps_map;
+typedef struct vfps_impedance vfps_impedance;
+typedef struct vfps_field vfps_field;
+typedef struct vfps_batch vfps_batch;
+
+/* ----------------------------------------------------------- context
+ * Replaces the OpenCL handler (src/CL/OpenCLHandler.cpp:23-92): one device,
+ * one in-order stream. */
+VFPS_API int vfps_create(vfps_ctx** ctx, int device);
+VFPS_API int vfps_destroy(vfps_ctx* ctx);
+VFPS_API const char* vfps_last_error(const vfps_ctx* ctx);
+/* OCLH::flush / finish: wait for all queued work of the context. */
+VFPS_API int vfps_synchronize(vfps_ctx* ctx);
+/* The context's cudaStream_t, for callers that order their own work. */
+VFPS_API void* vfps_stream(vfps_ctx* ctx);
+/* Device-side error word (bounded waits, watchdogs); 0 = none.  Reading it
+ * synchronises; *code is cleared afterwards. */
+VFPS_API int vfps_device_status(vfps_ctx* ctx, int* code);
+/* Pinned host buffers for asynchronous copies (no reference counterpart). */
+VFPS_API int vfps_host_alloc(vfps_ctx* ctx, size_t bytes, void** ptr);
+VFPS_API int vfps_host_free(vfps_ctx* ctx, void* ptr);
+
+/* -------------------------------------------------------- PhaseSpace
+ * PhaseSpace(qmin,qmax,qscale,pmin,pmax,pscale,oclh,charge,current,
+ *            filling,zoom,data), inc/PS/PhaseSpace.hpp:79-91 and
+ * src/PS/PhaseSpace.cpp:17-134.  axes = {qmin, qmax, qscale, pmin, pmax,
+ * pscale}; qscale is the "Meter" and pscale the "ElectronVolt" scale.
+ * filling[nb] must sum to 1 (else VFPS_ERR_INVALID_ARGUMENT).  data ==
+ * NULL creates the normalised Gaussian of width zoom, otherwise nb*n*n
+ * values are copied.  The static PhaseSpace::setSize(n, nb)
+ * (src/PS/PhaseSpace.cpp:428-443) becomes per-object sizes. */
+VFPS_API int vfps_ps_create(vfps_ctx* ctx, uint32_t nb, uint32_t n,
+                            const double axes[6], double charge,
+                            double current, const float* filling,
+                            double zoom, const float* data, vfps_ps** ps);
+/* copy constructor, src/PS/PhaseSpace.cpp:168-178 */
+VFPS_API int vfps_ps_copy(const vfps_ps* src, vfps_ps** ps);
+VFPS_API int vfps_ps_destroy(vfps_ps* ps);
+/* PhaseSpace::swap / operator= (src/PS/PhaseSpace.cpp:374-378,503-506):
+ * exchange or copy the density only. */
+VFPS_API int vfps_ps_swap(vfps_ps* a, vfps_ps* b);
+VFPS_API int vfps_ps_assign(vfps_ps* dst, const vfps_ps* src);
+/* getData() with a device->host copy / writing the density back
+ * (syncCLMem, src/PS/PhaseSpace.cpp:381-414). */
+VFPS_API int vfps_ps_download(vfps_ps* ps, float* data);
+VFPS_API int vfps_ps_upload(vfps_ps* ps, const float* data);
+/* Device pointer of the density (nb*n*n floats), for zero-copy callers. */
+VFPS_API float* vfps_ps_device_data(vfps_ps* ps);
+/* sizes and the axis rulers (inc/PS/Ruler.hpp:31-51): values[n], delta,
+ * zerobin of axis 0 (q) or 1 (p) */
+VFPS_API int vfps_ps_shape(const vfps_ps* ps, uint32_t* nb, uint32_t* n);
+VFPS_API int vfps_ps_axis(const vfps_ps* ps, int axis, float* values,
+                          float* delta, float* zerobin);
+/* updateXProjection / updateYProjection, src/PS/PhaseSpace.cpp:291-340
+ * (sums accumulated in FP64 on the device) */
+VFPS_API int vfps_ps_update_x_projection(vfps_ps* ps);
+VFPS_API int vfps_ps_update_y_projection(vfps_ps* ps);
+/* integrate / normalize / integrateAndNormalize,
+ * src/PS/PhaseSpace.cpp:200-239,342-372, inc/PS/PhaseSpace.hpp:222-226
+ * (FP64 on the device) */
+VFPS_API int vfps_ps_integrate(vfps_ps* ps);
+VFPS_API int vfps_ps_normalize(vfps_ps* ps);
+VFPS_API int vfps_ps_integrate_and_normalize(vfps_ps* ps);
+/* variance(axis) (src/PS/PhaseSpace.cpp:241-289): average and variance
+ * from the current projection of that axis. */
+VFPS_API int vfps_ps_variance(vfps_ps* ps, int axis);
+/* getProjection(axis) -> proj[nb*n]; setProjection(axis, bunch, proj) */
+VFPS_API int vfps_ps_get_projection(vfps_ps* ps, int axis, float* proj);
+VFPS_API int vfps_ps_set_projection(vfps_ps* ps, int axis, uint32_t bunch,
+                                    const float* proj);
+/* getBunchPopulation(), getIntegral() */
+VFPS_API int vfps_ps_get_filling(vfps_ps* ps, float* filling,
+                                 double* integral);
+/* getMoment(axis,0|1) and getBunchLength()/getEnergySpread() (rms) */
+VFPS_API int vfps_ps_get_moments(vfps_ps* ps, int axis, float* average,
+                                 float* variance, float* rms);
+
+/* ---------------------------------------------------------- SourceMaps
+ * Every map binds its input and output PhaseSpace at construction
+ * (inc/SM/SourceMap.hpp:53-72) and is applied with vfps_map_apply
+ * (SourceMap::apply(), inc/SM/SourceMap.hpp:79).  The interpolation
+ * weights are evaluated on the device; no per-cell table is stored. */
+
+/* RotationMap(in,out,xsize,ysize,angle,it,clamp,rotmapsize,oclh),
+ * inc/SM/RotationMap.hpp:40-45.  rotmapsize is 0 or xsize*ysize; clamping
+ * needs cubic interpolation and rotmapsize > 0. */
+VFPS_API int vfps_rotation_map_create(vfps_ps* in, vfps_ps* out,
+                                      uint32_t xsize, uint32_t ysize,
+                                      float angle, int it, int clamp,
+                                      uint32_t rotmapsize, vfps_map** map);
+/* KickMap(in,out,it,clamp,axis,oclh), inc/SM/KickMap.hpp:34-38; the
+ * offsets start at 0.  Clamping of kicks is not implemented by the
+ * reference's CPU path (src/SM/KickMap.cpp:42-44); here it clamps to the
+ * two nearest source cells, the rule of its OpenCL kernels (:80-85). */
+VFPS_API int vfps_kick_map_create(vfps_ps* in, vfps_ps* out, int it,
+                                  int clamp, int axis, vfps_map** map);
+/* KickMap::swapOffset (inc/SM/KickMap.hpp:54-55): count = n (x-kick) or
+ * nb*n (y-kick, one row of offsets per bunch) values in mesh units. */
+VFPS_API int vfps_kick_map_set_offset(vfps_map* map, const float* offset,
+                                      size_t count);
+/* KickMap::getForce (inc/SM/KickMap.hpp:47-48) */
+VFPS_API int vfps_kick_map_get_offset(vfps_map* map, float* offset,
+                                      size_t count);
+/* DriftMap(in,out,slip,E0,it,clamp,oclh), inc/SM/DriftMap.hpp:17-24 */
+VFPS_API int vfps_drift_map_create(vfps_ps* in, vfps_ps* out,
+                                   const float* slip, uint32_t nslip,
+                                   float e0, int it, int clamp,
+                                   vfps_map** map);
+/* RFKickMap, linear RF (inc/SM/RFKickMap.hpp:17-23) */
+VFPS_API int vfps_rf_kick_map_create_linear(vfps_ps* in, vfps_ps* out,
+                                            float angle, float f_rf, int it,
+                                            int clamp, vfps_map** map);
+/* RFKickMap, sinusoidal RF (inc/SM/RFKickMap.hpp:26-34) */
+VFPS_API int vfps_rf_kick_map_create(vfps_ps* in, vfps_ps* out,
+                                     float revolutionpart, float v_rf,
+                                     float f_rf, float v0, int it, int clamp,
+                                     vfps_map** map);
+/* FokkerPlanckMap(in,out,xsize,ysize,fptype,fptrack,e1,derivation,oclh),
+ * inc/SM/FokkerPlanckMap.hpp:56-64 */
+VFPS_API int vfps_fokker_planck_map_create(vfps_ps* in, vfps_ps* out,
+                                           uint32_t xsize, uint32_t ysize,
+                                           int fptype, int fptrack, float e1,
+                                           int derivation, vfps_map** map);
+/* Identity(in,out,oclh), inc/SM/Identity.hpp:29-34 */
+VFPS_API int vfps_identity_map_create(vfps_ps* in, vfps_ps* out,
+                                      vfps_map** map);
+/* WakePotentialMap(in,out,field,it,clamp,oclh),
+ * inc/SM/WakePotentialMap.hpp:20-26 */
+VFPS_API int vfps_wake_potential_map_create(vfps_ps* in, vfps_ps* out,
+                                            vfps_field* field, int it,
+                                            int clamp, vfps_map** map);
+/* WakeKickMap::update (inc/SM/WakeKickMap.hpp:38,
+ * src/SM/WakePotentialMap.cpp:34-50): wake potential -> kick offsets. */
+VFPS_API int vfps_wake_map_update(vfps_map* map);
+/* SourceMap::apply() */
+VFPS_API int vfps_map_apply(vfps_map* map);
+/* SourceMap::applyToAll(particles) (src/SM/SourceMap.cpp:111-117):
+ * pos = {x0, y0, x1, y1, ...} in mesh coordinates, updated in place on the
+ * host (particle tracking is for display, as in the reference). */
+VFPS_API int vfps_map_apply_to(vfps_map* map, float* pos, size_t count);
+VFPS_API int vfps_map_destroy(vfps_map* map);
+
+/* ---------------------------------------------------------- Impedance
+ * Impedance (inc/Z/Impedance.hpp:29-113): a complex table of nfreqs
+ * entries over [0, f_max].  Model tables are computed on the device in
+ * FP64 and stored as complex float. */
+VFPS_API int vfps_impedance_create(vfps_ctx* ctx, const float* z,
+                                   size_t nfreqs, double f_max,
+                                   vfps_impedance** imp);
+/* FreeSpaceCSR(n,f_rev,f_max), src/Z/FreeSpaceCSR.cpp:10-43 */
+VFPS_API int vfps_impedance_free_space_csr(vfps_ctx* ctx, size_t n,
+                                           float f_rev, float f_max,
+                                           vfps_impedance** imp);
+/* ParallelPlatesCSR(n,f0,f_max,g), src/Z/ParallelPlatesCSR.cpp:12-70 */
+VFPS_API int vfps_impedance_parallel_plates_csr(vfps_ctx* ctx, size_t n,
+                                                float f0, float f_max,
+                                                double g,
+                                                vfps_impedance** imp);
+/* ResistiveWall(n,f0,f_max,L,s,xi,b), src/Z/ResistiveWall.cpp:11-57 */
+VFPS_API int vfps_impedance_resistive_wall(vfps_ctx* ctx, size_t n,
+                                           float f0, float f_max, double L,
+                                           double s, double xi, double b,
+                                           vfps_impedance** imp);
+/* ConstImpedance(n,f_max,Z), src/Z/ConstImpedance.cpp:10-28 */
+VFPS_API int vfps_impedance_const(vfps_ctx* ctx, size_t n, float f_max,
+                                  float re, float im, vfps_impedance** imp);
+/* CollimatorImpedance(n,f_max,outer,inner),
+ * src/Z/CollimatorImpedance.cpp:12-25 */
+VFPS_API int vfps_impedance_collimator(vfps_ctx* ctx, size_t n, float f_max,
+                                       double outer, double inner,
+                                       vfps_impedance** imp);
+/* Impedance(datafile,f_max), src/Z/Impedance.cpp:53-59,94-111 */
+VFPS_API int vfps_impedance_from_file(vfps_ctx* ctx, const char* path,
+                                      double f_max, vfps_impedance** imp);
+/* makeImpedance (src/Z/ImpedanceFactory.cpp:21-84).  *imp is NULL when no
+ * contribution is selected (the reference returns nullptr). */
+VFPS_API int vfps_make_impedance(vfps_ctx* ctx, size_t nfreqs, float fmax,
+                                 double r_bend, double frev, double gap,
+                                 int use_csr, double s, double xi,
+                                 double inner_coll_radius,
+                                 const char* impedance_file,
+                                 vfps_impedance** imp);
+/* operator+= (src/Z/Impedance.cpp:67-76) and copy constructor */
+VFPS_API int vfps_impedance_add(vfps_impedance* dst,
+                                const vfps_impedance* rhs);
+VFPS_API int vfps_impedance_copy(const vfps_impedance* src,
+                                 vfps_impedance** imp);
+VFPS_API int vfps_impedance_swap(vfps_impedance* a, vfps_impedance* b);
+/* nFreqs(), data(), getRuler()->max() */
+VFPS_API int vfps_impedance_get(const vfps_impedance* imp, float* z,
+                                size_t* nfreqs, double* f_max);
+VFPS_API int vfps_impedance_destroy(vfps_impedance* imp);
+
+/* ------------------------------------------------------- ElectricField
+ * ElectricField(ps,impedance,bucketnumbers,spacing_bins,oclh,f_rev,
+ * revolutionpart,wakescaling), inc/PS/ElectricField.hpp:49-56.
+ * buckets[nb] are the bucket numbers of the bunches of ps.  wakescaling 0
+ * gives a field without wake potential. */
+VFPS_API int vfps_field_create(vfps_ps* ps, const vfps_impedance* imp,
+                               const uint32_t* buckets, uint32_t spacing_bins,
+                               double f_rev, double revolutionpart,
+                               double wakescaling, vfps_field** field);
+/* The wake-potential constructor (inc/PS/ElectricField.hpp:81-103):
+ * wakescaling = Ib dt c / qscale / (dp sigma_delta E0). */
+VFPS_API int vfps_field_create_wake(vfps_ps* ps, const vfps_impedance* imp,
+                                    const uint32_t* buckets,
+                                    uint32_t spacing_bins, double f_rev,
+                                    double revolutionpart, double ib,
+                                    double e0, double sigma_delta, double dt,
+                                    vfps_field** field);
+/* padBunchProfiles (src/PS/ElectricField.cpp:255-263) and
+ * getPaddedBunchProfiles(): padded[nmax] */
+VFPS_API int vfps_field_pad_bunch_profiles(vfps_field* field);
+VFPS_API int vfps_field_get_padded_profiles(vfps_field* field,
+                                            float* padded);
+/* wakePotential() (src/PS/ElectricField.cpp:186-253): from the phase
+ * space's current x projection; result stays on the device. */
+VFPS_API int vfps_field_wake_potential(vfps_field* field);
+/* getWakePotentials(): wake[nb*n] */
+VFPS_API int vfps_field_get_wake_potential(vfps_field* field, float* wake);
+/* getWakeScaling() (wakescaling/nmax), getNMax() */
+VFPS_API int vfps_field_info(const vfps_field* field, float* wakescale,
+                             size_t* nmax);
+/* updateCSR(fc) (src/PS/ElectricField.cpp:133-184). */
+VFPS_API int vfps_field_update_csr(vfps_field* field, float fc);
+/* getCSRSpectrum() spectrum[nb*nmax] and getCSRPower() power[nb]; either
+ * may be NULL.  factor4Watts (inc/PS/ElectricField.hpp:203-208) converts
+ * the power to W. */
+VFPS_API int vfps_field_get_csr(vfps_field* field, float* spectrum,
+                                float* power, double* factor4watts);
+VFPS_API int vfps_field_destroy(vfps_field* field);
+
+/* ------------------------------------------------------------ batches
+ * No reference counterpart: many independent single-bunch simulations
+ * (current scans, uneven grid sizes) stepped together by fused kernels
+ * captured in a CUDA graph.  Each bunch follows the reference solver step
+ * (src/main.cpp:948-1053 for chain 0, the rotation scheme of
+ * test/TestRotationMap.cpp for chain 1). */
+typedef struct {
+    uint32_t n;            /* mesh side of this bunch */
+    int32_t chain;         /* 0: wake, RF y-kick, drift x-kick, FP
+                              1: rotation, wake y-kick, FP */
+    int32_t it;            /* interpolation points (2, 3, 4) */
+    int32_t clamp;         /* rotation clamp (chain 1, cubic) */
+    double axes[6];        /* qmin, qmax, qscale, pmin, pmax, pscale */
+    double zoom;           /* width of the initial Gaussian */
+    double angle;          /* chain 1: rotation per step */
+    int32_t rf_linear;     /* chain 0: 1 linear, 0 sinusoidal RF */
+    double rf_angle;       /* linear RF: angle per step */
+    double rf_revpart, rf_vrf, rf_v0, rf_bl2phase, rf_phase;
+    double slip[3];        /* drift slip terms (src/main.cpp:663-664) */
+    int32_t nslip;
+    double e0;             /* beam energy (eV) */
+    double e1;             /* FP decrement 2/(fs td steps); <= 0: none */
+    int32_t fptype, derivation;
+    double wakescaling;    /* ElectricField wakescaling; 0: no wake */
+    int32_t renormalize;   /* >0 every n steps, 0 once, <0 never */
+    int32_t impedance;     /* index into the impedance list of the batch */
+} vfps_bunch_desc;
+
+/* imps[nimp]: impedance tables shared by the bunches that name them;
+ * each table's nfreqs must be >= 2 n of its bunches.  data == NULL starts
+ * every bunch from its Gaussian. */
+VFPS_API int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
+                               const vfps_bunch_desc* desc,
+                               const vfps_impedance* const* imps,
+                               uint32_t nimp, const float* data,
+                               vfps_batch** batch);
+/* Advance every bunch by nsteps solver steps (device only). */
+VFPS_API int vfps_batch_step(vfps_batch* batch, uint64_t nsteps);
+/* End-to-end: densities from host memory in, nsteps steps, densities
+ * (and optionally profiles [total cells of all profiles] and fillings
+ * [nb]) back to host memory.  Either input or output may be NULL. */
+VFPS_API int vfps_batch_run(vfps_batch* batch, const float* density_in,
+                            uint64_t nsteps, float* density_out,
+                            float* profiles_out, float* filling_out);
+/* Offsets of bunch b in the packed density/profile arrays. */
+VFPS_API int vfps_batch_layout(const vfps_batch* batch, uint32_t b,
+                               size_t* density_offset, size_t* profile_offset);
+VFPS_API int vfps_batch_download(vfps_batch* batch, float* density);
+VFPS_API int vfps_batch_upload(vfps_batch* batch, const float* density);
+VFPS_API int vfps_batch_get_profiles(vfps_batch* batch, float* profiles);
+VFPS_API int vfps_batch_get_filling(vfps_batch* batch, double* filling);
+VFPS_API int vfps_batch_get_wake(vfps_batch* batch, float* wake);
+/* kernel launches per solver step (for launch accounting) */
+VFPS_API int vfps_batch_info(const vfps_batch* batch, uint32_t* launches,
+                             uint32_t* tile_rows);
+VFPS_API int vfps_batch_destroy(vfps_batch* batch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VFPS_H */

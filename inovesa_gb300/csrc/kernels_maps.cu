@@ -1,0 +1,207 @@
+// Plain (one map per launch) SourceMap kernels.  Weights are evaluated in
+// registers from the source coordinate -- the reference's per-cell
+// (index, weight) tables (8 B per tap) are never materialised.
+//
+//  k_rotation  RotationMap::genHInfo + apply (src/SM/RotationMap.cpp:97-260)
+//  k_kick_y    KickMap y-kick, one CTA per mesh row (src/SM/KickMap.cpp:244-266)
+//  k_kick_x    KickMap x-kick (src/SM/KickMap.cpp:221-242)
+//  k_fp        FokkerPlanckMap::apply (src/SM/FokkerPlanckMap.cpp:170-213)
+#include <cfloat>
+
+#include "vfps_internal.cuh"
+
+namespace vfps {
+namespace {
+
+using namespace dev;
+
+__global__ void k_rotation(const float* __restrict__ in,
+                           float* __restrict__ out, uint32_t n,
+                           const float* __restrict__ qv,
+                           const float* __restrict__ pv, float dq, float dp,
+                           float zbq, float zbp, float cs, float sn, int it,
+                           int clamp)
+{
+    const uint32_t y0 = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t x0 = blockIdx.y;
+    if (y0 >= n) {
+        return;
+    }
+    const size_t nxy = size_t(n) * n;
+    const float* src = in + blockIdx.z * nxy;
+    const float q = qv[x0], p = pv[y0];
+    const float x1r = fadd(fdiv(fsub(fmul(cs, q), fmul(sn, p)), dq), zbq);
+    const float y1r = fadd(fdiv(fadd(fmul(sn, q), fmul(cs, p)), dp), zbp);
+    int x1 = 0, y1 = 0;
+    float xf, yf;
+    const bool okx = base_index(x1r, n, &x1, &xf);
+    const bool oky = base_index(y1r, n, &y1, &yf);
+    const bool ok = okx && oky;
+    float value = 0.f;
+    float icq[4], icp[4];
+    const int h = (it - 1) / 2;
+    if (ok) {
+        coefficients(icq, xf, it);
+        coefficients(icp, yf, it);
+        for (int i1 = 0; i1 < it; i1++) {
+            const int i0 = x1 + i1 - h;
+            for (int j1 = 0; j1 < it; j1++) {
+                const int j0 = y1 + j1 - h;
+                if (i0 >= 0 && i0 < int(n) && j0 >= 0 && j0 < int(n)) {
+                    value = fadd(value, fmul(__ldg(src + size_t(i0) * n + j0),
+                                             fmul(icq[i1], icp[j1])));
+                }
+            }
+        }
+    }
+    if (clamp) {
+        // src/SM/RotationMap.cpp:159-172: range of the 2x2 nearest taps,
+        // starting from FLT_MIN / FLT_MAX; taps off the mesh read cell 0.
+        float ceil_v = FLT_MIN, flor_v = FLT_MAX;
+        for (int i1 = 1; i1 <= 2; i1++) {
+            for (int j1 = 1; j1 <= 2; j1++) {
+                const int i0 = x1 + i1 - h, j0 = y1 + j1 - h;
+                const bool in_mesh = ok && i0 >= 0 && i0 < int(n) && j0 >= 0
+                                     && j0 < int(n);
+                const float v = __ldg(src + (in_mesh ? size_t(i0) * n + j0 : 0));
+                ceil_v = (ceil_v < v) ? v : ceil_v;
+                flor_v = (v < flor_v) ? v : flor_v;
+            }
+        }
+        const float t = (value < ceil_v) ? value : ceil_v;
+        value = (t < flor_v) ? flor_v : t;
+    }
+    out[blockIdx.z * nxy + size_t(x0) * n + y0] = value;
+}
+
+// clamp of a kick to its two nearest source cells (the rule of the
+// reference's OpenCL kick kernels, src/SM/KickMap.cpp:80-85)
+__device__ __forceinline__ float clamp2(float value, const float* line,
+                                        size_t stride, int base, int n)
+{
+    float hi = -FLT_MAX, lo = FLT_MAX;
+    bool any = false;
+    for (int k = 0; k < 2; k++) {
+        const int s = base + k;
+        if (s >= 0 && s < n) {
+            const float v = __ldg(line + size_t(s) * stride);
+            hi = fmaxf(hi, v);
+            lo = fminf(lo, v);
+            any = true;
+        }
+    }
+    return any ? fminf(fmaxf(value, lo), hi) : value;
+}
+
+// one CTA per (bunch, row x); offsets[b*n + x] in mesh units
+__global__ void k_kick_y(const float* __restrict__ in, float* __restrict__ out,
+                         const float* __restrict__ offsets, uint32_t n, int it,
+                         int clamp)
+{
+    const uint32_t row = blockIdx.x;
+    const KickStencil s = kick_stencil(offsets[row], n, it);
+    const float* src = in + size_t(row) * n;
+    float* dst = out + size_t(row) * n;
+    const int h = (it - 1) / 2;
+    for (uint32_t y = threadIdx.x; y < n; y += blockDim.x) {
+        float value = 0.f;
+        for (int j = 0; j < it; j++) {
+            const int ys = int(y) + s.shift[j];
+            if (s.valid[j] && ys >= 0 && ys < int(n)) {
+                value = fadd(value, fmul(__ldg(src + ys), s.w[j]));
+            }
+        }
+        if (clamp) {
+            value = clamp2(value, src, 1, int(y) + s.shift[h], int(n));
+        }
+        dst[y] = value;
+    }
+}
+
+// thread per cell; offsets[y] shared by all bunches
+__global__ void k_kick_x(const float* __restrict__ in, float* __restrict__ out,
+                         const float* __restrict__ offsets, uint32_t n, int it,
+                         int clamp)
+{
+    const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t x = blockIdx.y;
+    if (y >= n) {
+        return;
+    }
+    const size_t nxy = size_t(n) * n;
+    const float* src = in + blockIdx.z * nxy;
+    const KickStencil s = kick_stencil(offsets[y], n, it);
+    float value = 0.f;
+    for (int j = 0; j < it; j++) {
+        const int xs = int(x) + s.shift[j];
+        if (s.valid[j] && xs >= 0 && xs < int(n)) {
+            value = fadd(value, fmul(__ldg(src + size_t(xs) * n + y), s.w[j]));
+        }
+    }
+    if (clamp) {
+        value = clamp2(value, src + y, n, int(x) + s.shift[(it - 1) / 2],
+                       int(n));
+    }
+    out[blockIdx.z * nxy + size_t(x) * n + y] = value;
+}
+
+// thread per cell; stencil table idx/w [n][ip] shared by every row
+__global__ void k_fp(const float* __restrict__ in, float* __restrict__ out,
+                     const uint32_t* __restrict__ idx,
+                     const float* __restrict__ w, uint32_t n, int ip)
+{
+    const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t x = blockIdx.y;
+    if (y >= n) {
+        return;
+    }
+    const size_t row = (blockIdx.z * size_t(n) + x) * n;
+    float value = 0.f;
+    for (int j = 0; j < ip; j++) {
+        value = fadd(value, fmul(__ldg(in + row + idx[y * ip + j]),
+                                 w[y * ip + j]));
+    }
+    out[row + y] = value;
+}
+
+}  // namespace
+
+void launch_rotation(const vfps_map* m)
+{
+    const vfps_ps* in = m->in;
+    const uint32_t n = in->n;
+    dim3 grid((n + 127) / 128, n, in->nb);
+    k_rotation<<<grid, 128, 0, in->ctx->stream>>>(
+        in->data.p, m->out->data.p, n, in->axisv[0].p, in->axisv[1].p,
+        in->ax[0].delta, in->ax[1].delta, in->ax[0].zerobin, in->ax[1].zerobin,
+        m->cs, m->sn, m->it, m->clamp);
+    VFPS_LAUNCHED();
+}
+
+void launch_kick(const vfps_map* m, const float* offset)
+{
+    const vfps_ps* in = m->in;
+    const uint32_t n = in->n;
+    if (m->axis == VFPS_AXIS_Y) {
+        const int threads = n >= 256 ? 256 : ((n + 31) / 32) * 32;
+        k_kick_y<<<in->nb * n, threads, 0, in->ctx->stream>>>(
+            in->data.p, m->out->data.p, offset, n, m->it, m->clamp);
+    } else {
+        dim3 grid((n + 127) / 128, n, in->nb);
+        k_kick_x<<<grid, 128, 0, in->ctx->stream>>>(
+            in->data.p, m->out->data.p, offset, n, m->it, m->clamp);
+    }
+    VFPS_LAUNCHED();
+}
+
+void launch_fp(const vfps_map* m)
+{
+    const vfps_ps* in = m->in;
+    const uint32_t n = in->n;
+    dim3 grid((n + 127) / 128, n, in->nb);
+    k_fp<<<grid, 128, 0, in->ctx->stream>>>(in->data.p, m->out->data.p,
+                                            m->fp_idx.p, m->fp_w.p, n, m->ip);
+    VFPS_LAUNCHED();
+}
+
+}  // namespace vfps

@@ -1,0 +1,344 @@
+// Internal declarations of libvfps: objects behind the C ABI, RAII device
+// buffers, error plumbing and device helpers shared by the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "vfps.h"
+
+namespace vfps {
+
+// ------------------------------------------------------------ errors
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define VFPS_CUDA(call)                                                   \
+    do {                                                                  \
+        cudaError_t e_ = (call);                                          \
+        if (e_ != cudaSuccess) {                                          \
+            throw ::vfps::Error(                                          \
+                e_ == cudaErrorMemoryAllocation ? VFPS_ERR_OUT_OF_MEMORY  \
+                                                : VFPS_ERR_CUDA,          \
+                std::string(#call) + ": " + cudaGetErrorString(e_));      \
+        }                                                                 \
+    } while (0)
+
+#define VFPS_REQUIRE(cond, msg)                                           \
+    do {                                                                  \
+        if (!(cond)) {                                                    \
+            throw ::vfps::Error(VFPS_ERR_INVALID_ARGUMENT, (msg));        \
+        }                                                                 \
+    } while (0)
+
+#define VFPS_LAUNCHED() VFPS_CUDA(cudaGetLastError())
+
+// ----------------------------------------------------- device buffers
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    explicit DevBuf(size_t count) { alloc(count); }
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    DevBuf(DevBuf&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf& operator=(DevBuf&& o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        if (count) {
+            VFPS_CUDA(cudaMalloc(&p, count * sizeof(T)));
+        }
+        n = count;
+    }
+    void release() noexcept
+    {
+        if (p) {
+            cudaFree(p);
+        }
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return n * sizeof(T); }
+    void swap(DevBuf& o) noexcept
+    {
+        std::swap(p, o.p);
+        std::swap(n, o.n);
+    }
+};
+
+// --------------------------------------------------------------- axis
+// Ruler (inc/PS/Ruler.hpp:31-51) in float, as the reference keeps it.
+struct Axis {
+    uint32_t n = 0;
+    float min = 0, max = 0, delta = 0, zerobin = 0, scale = 1;
+    std::vector<float> v;
+};
+Axis make_axis(uint32_t n, float mn, float mx, float scale);
+
+}  // namespace vfps
+
+// ----------------------------------------------------- C ABI objects
+struct vfps_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    int* d_status = nullptr;   // device error word
+    int sm_count = 0;
+};
+
+struct vfps_ps {
+    vfps_ctx* ctx = nullptr;
+    uint32_t nb = 0, n = 0;
+    double charge = 0, current = 0;
+    vfps::Axis ax[2];
+    std::vector<float> filling_set;
+    vfps::DevBuf<float> data;        // [nb][n][n]
+    vfps::DevBuf<float> proj[2];     // [nb][n] per axis
+    vfps::DevBuf<double> proj64;     // x projection, FP64
+    vfps::DevBuf<float> ws;          // Simpson weights [n]
+    vfps::DevBuf<float> axisv[2];    // axis values [n]
+    vfps::DevBuf<float> fillset;     // [nb]
+    vfps::DevBuf<double> filling;    // [nb] + integral at [nb]
+    vfps::DevBuf<float> moments;     // [2][3][nb]: avg, var, rms
+};
+
+enum MapKind {
+    MAP_ROTATION,
+    MAP_KICK,
+    MAP_FP,
+    MAP_IDENTITY
+};
+
+struct vfps_map {
+    MapKind kind = MAP_IDENTITY;
+    vfps_ps* in = nullptr;
+    vfps_ps* out = nullptr;
+    int it = 4;
+    int clamp = 0;
+    // rotation
+    float angle = 0, cs = 1, sn = 0;
+    // kick
+    int axis = 1;
+    vfps::DevBuf<float> offset;      // x-kick: [n]; y-kick: [nb][n]
+    const float* offset_src = nullptr;  // wake map: field's wake buffer
+    vfps_field* field = nullptr;
+    std::vector<float> host_offset;  // mirror for applyTo / getForce
+    bool host_offset_valid = true;
+    // Fokker-Planck
+    int ip = 0;
+    int fptrack = 0;
+    float e1 = 0;
+    vfps::DevBuf<uint32_t> fp_idx;
+    vfps::DevBuf<float> fp_w;
+    std::vector<uint32_t> h_fp_idx;
+    std::vector<float> h_fp_w;
+};
+
+struct vfps_impedance {
+    vfps_ctx* ctx = nullptr;
+    size_t nfreqs = 0;
+    double f_max = 0;
+    vfps::DevBuf<float> z;           // interleaved re, im
+};
+
+struct vfps_field {
+    vfps_ps* ps = nullptr;
+    const vfps_impedance* imp = nullptr;
+    vfps::DevBuf<float> z;           // private copy of the table
+    size_t nmax = 0;
+    uint32_t spacing = 0;
+    std::vector<uint32_t> buckets;
+    vfps::DevBuf<uint32_t> d_pos;    // bucket * spacing per bunch
+    double f_rev = 0, revpart = 1;
+    float wakescale = 0;             // wakescaling / nmax
+    bool has_wake = false;
+    vfps::DevBuf<float> wtab;        // Toeplitz kernel w[d], d in [0,nmax)
+    vfps::DevBuf<float> wake;        // [nb][n]
+    vfps::DevBuf<float> padded;      // [nmax]
+    // CSR
+    vfps::DevBuf<float> twiddle;     // [nmax] (cos, sin) pairs
+    vfps::DevBuf<float> csr_coef;    // [nmax/2+1]
+    vfps::DevBuf<float> spectrum;    // [nb][nmax]
+    vfps::DevBuf<double> power;      // [nb]
+    float csr_fc = -1;
+    bool csr_ready = false;
+    float freq_delta = 0;
+    double freq_scale = 0;
+    double factor4watts = 0;
+};
+
+// ----------------------------------------------------- launch wrappers
+namespace vfps {
+
+void set_status(vfps_ctx* ctx, int code);  // host-side helper
+
+void launch_fill_gaussian(vfps_ps* ps, const float* gx, const float* gy);
+void launch_project_x(vfps_ps* ps, const float* data);
+void launch_project_y(vfps_ps* ps);
+void launch_integrate(vfps_ps* ps);
+void launch_normalize(vfps_ps* ps);
+void launch_moments(vfps_ps* ps, int axis);
+
+void launch_rotation(const vfps_map* m);
+void launch_kick(const vfps_map* m, const float* offset);
+void launch_fp(const vfps_map* m);
+
+void launch_wake_table(vfps_field* f);
+void launch_wake_table_raw(vfps_ctx* ctx, const float* z, size_t nmax,
+                           float* out);
+void launch_wake(vfps_field* f);
+void launch_pad(vfps_field* f);
+void launch_csr(vfps_field* f);
+
+void launch_z_model(vfps_ctx* ctx, int model, size_t n, const double* prm,
+                    float* out);
+void launch_z_add(vfps_ctx* ctx, float* dst, const float* src, size_t n);
+
+}  // namespace vfps
+
+// ------------------------------------------------------ device helpers
+// Float arithmetic with the reference's operation order and rounding
+// (no contraction into FMA), so that stencils agree with its CPU build.
+namespace vfps {
+namespace dev {
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// calcCoefficiants (src/SM/SourceMap.cpp:142-170); x/2 == x*0.5 exactly.
+__device__ __forceinline__ void coefficients(float* ic, float f, int it)
+{
+    switch (it) {
+    case 1:
+        ic[0] = 1.f;
+        break;
+    case 2:
+        ic[0] = fsub(1.f, f);
+        ic[1] = f;
+        break;
+    case 3:
+        ic[0] = fmul(fmul(f, fsub(f, 1.f)), 0.5f);
+        ic[1] = fsub(1.f, fmul(f, f));
+        ic[2] = fmul(fmul(f, fadd(f, 1.f)), 0.5f);
+        break;
+    default:
+        ic[0] = fmul(fmul(fmul(fsub(f, 1.f), fsub(f, 2.f)), f),
+                     static_cast<float>(-1. / 6.));
+        ic[1] = fmul(fmul(fmul(fadd(f, 1.f), fsub(f, 1.f)), fsub(f, 2.f)),
+                     0.5f);
+        ic[2] = fmul(fmul(fmul(fsub(2.f, f), f), fadd(f, 1.f)), 0.5f);
+        ic[3] = fmul(fmul(fmul(f, fadd(f, 1.f)), fsub(f, 1.f)),
+                     static_cast<float>(1. / 6.));
+        break;
+    }
+}
+
+// truncated base index of a source coordinate, as modf + static_cast<>
+// to uint32 do on x86-64: values <= -1 and >= size are out of range.
+__device__ __forceinline__ bool base_index(float v, uint32_t size, int* base,
+                                           float* frac)
+{
+    const float t = truncf(v);
+    *frac = v - t;  // exact
+    if (!(t >= 0.f) || !(t < static_cast<float>(size))) {
+        return false;
+    }
+    *base = static_cast<int>(t);
+    return true;
+}
+
+// KickMap::updateSM (src/SM/KickMap.cpp:339-389) for one row/column:
+// source index offset (tap j reads cell i + shift[j]) and weight, with
+// dropped taps marked by weight 0 and valid = false.
+struct KickStencil {
+    int shift[4];
+    float w[4];
+    bool valid[4];
+};
+
+__device__ __forceinline__ KickStencil kick_stencil(float offset, uint32_t n,
+                                                    int it)
+{
+    KickStencil s;
+    const float poffs = fadd(static_cast<float>(n / 2), offset);
+    int jd;
+    float f;
+    const bool ok = base_index(poffs, n, &jd, &f);
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+    if (ok) {
+        coefficients(c, f, it);
+    }
+    const int h = (it - 1) / 2;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int j0 = jd + j - h;
+        s.valid[j] = ok && j < it && j0 >= 0 && j0 < static_cast<int>(n);
+        s.w[j] = s.valid[j] ? c[j] : 0.f;
+        s.shift[j] = j0 - static_cast<int>(n / 2);
+    }
+    return s;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+// block-wide FP64 sum (blockDim multiple of 32, <= 1024); result valid in
+// thread 0.
+__device__ __forceinline__ double block_sum(double v, double* scratch32)
+{
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) {
+        scratch32[warp] = v;
+    }
+    __syncthreads();
+    v = 0;
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        v = lane < nw ? scratch32[lane] : 0.0;
+        v = warp_sum(v);
+    }
+    __syncthreads();
+    return v;
+}
+
+}  // namespace dev
+}  // namespace vfps

@@ -23,3 +23,15 @@ def golden():
     with open(os.path.join(ROOT, "tests", "golden",
                            "reference_tests.json")) as f:
         return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def gpu_ctx():
+    """CUDA context of libvfps on device 0 (built in-tree first)."""
+    from inovesa_gb300.build import build
+    build()
+    from inovesa_gb300 import vfps
+    ctx = vfps.Context(0)
+    yield ctx
+    ctx.synchronize()
+    assert ctx.device_status() == 0

@@ -1,0 +1,138 @@
+"""Whole solver steps against the FP64 oracle's solver loop.
+
+Tolerance: the metric's bar, relative L1 of the density <= 1e-4 against
+FP64, checked after tens to hundreds of steps; profiles and wakes within
+the same bound.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from inovesa_gb300 import params as P
+from inovesa_gb300 import vfps as V
+from inovesa_gb300.solver import PlainSolver
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def rel_l1(a, b):
+    return float(np.abs(np.asarray(a, np.float64) - b).sum()
+                 / np.abs(np.asarray(b, np.float64)).sum())
+
+
+def oracle_sim(p, chain, Ib, Z, it=None, clamp=False, data=None):
+    d = P.fill_desc(oracle.BunchDesc(), p, chain, Ib=Ib, it=it, clamp=clamp)
+    return oracle.Sim([d], Z=Z, data=data, dtype=np.float64)
+
+
+CASES = [
+    # (grid, steps per period, gap, S, chain, it, clamp, renormalize)
+    (128, 500, -1.0, 0.05, 0, 4, False, 0),
+    (128, 500, -1.0, 0.05, 1, 4, True, 0),
+    (128, 1000, 0.0318, 0.8, 0, 3, False, 10),
+    (96, 400, 0.0318, 1.2, 1, 2, False, -1),
+]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_plain_loop(gpu_ctx, case):
+    n, spt, gap, S, chain, it, clamp, renorm = case
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=gap,
+                 S_csr=S, RenormalizeCharge=renorm, InterpolationPoints=it)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    s = PlainSolver(gpu_ctx, p, chain=chain, wake_impedance=z, it=it,
+                    clamp=clamp)
+    ref = oracle_sim(p, chain, p["Ib"], z.data(), it=it, clamp=clamp)
+    for block in range(3):
+        s.step(40)
+        ref.step(40)
+        assert rel_l1(s.density(), ref.density(0)) <= TOL, block
+        assert rel_l1(s.profile(), ref.profile(0)) <= TOL
+    wk = s.wake_field.getWakePotentials()[0]
+    assert np.abs(wk - ref.wake(0)).sum() <= TOL * np.abs(ref.wake(0)).sum()
+
+
+def make_batch(ctx, specs, z_by_n):
+    """specs: list of (p, chain, Ib, it, clamp); one impedance per mesh
+    size."""
+    sizes = sorted(z_by_n)
+    descs, zs = [], [z_by_n[k] for k in sizes]
+    for p, chain, ib, it, clamp in specs:
+        d = P.fill_desc(V.BunchDesc(), p, chain, Ib=ib,
+                        impedance=sizes.index(p["ps_bins"]), it=it,
+                        clamp=clamp)
+        descs.append(d)
+    return V.BunchBatch(ctx, descs, zs)
+
+
+def test_batch_matches_oracle(gpu_ctx):
+    specs, z_by_n, zdata = [], {}, {}
+    for n in (64, 128):
+        p0 = P.derive(GridSize=n, StepsPerTs=500, padding=2.0,
+                      VacuumGap=0.0318)
+        z_by_n[n] = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p0))
+        zdata[n] = z_by_n[n].data()
+    for k, (n, chain, it, clamp, S) in enumerate([
+            (128, 0, 4, False, 0.05), (128, 0, 4, False, 1.0),
+            (64, 0, 3, False, 0.5), (128, 1, 4, True, 0.3),
+            (64, 1, 2, False, 0.9), (128, 0, 2, False, 1.4)]):
+        p = P.derive(GridSize=n, StepsPerTs=500, padding=2.0,
+                     VacuumGap=0.0318, S_csr=S,
+                     RenormalizeCharge=(5 if k == 1 else 0))
+        specs.append((p, chain, p["Ib"], it, clamp))
+    b = make_batch(gpu_ctx, specs, z_by_n)
+    refs = [oracle_sim(p, ch, ib, zdata[p["ps_bins"]], it=it, clamp=cl)
+            for p, ch, ib, it, cl in specs]
+    for blk in range(3):
+        b.step(25)
+        for r in refs:
+            r.step(25)
+        dens = b.download()
+        for i, r in enumerate(refs):
+            off, _ = b.layout(i)
+            n = specs[i][0]["ps_bins"]
+            got = dens[off:off + n * n].reshape(n, n)
+            assert rel_l1(got, r.density(0)) <= TOL, (blk, i)
+            assert rel_l1(b.profile(i), r.profile(0)) <= TOL, (blk, i)
+    f = b.filling()
+    for i, r in enumerate(refs):
+        assert abs(f[i] - 1) < 5e-3
+    assert gpu_ctx.device_status() == 0
+
+
+def test_batch_equals_plain_loop(gpu_ctx):
+    """The fused kernel and the one-map-per-launch loop agree."""
+    n = 128
+    p = P.derive(GridSize=n, StepsPerTs=500, padding=2.0, VacuumGap=-1.0,
+                 S_csr=0.6)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    for chain in (0, 1):
+        s = PlainSolver(gpu_ctx, p, chain=chain, wake_impedance=z)
+        b = make_batch(gpu_ctx, [(p, chain, p["Ib"], 4, False)], {n: z})
+        s.step(64)
+        b.step(64)
+        assert rel_l1(b.density(0), s.density()) <= 2e-5
+
+
+def test_batch_run_end_to_end(gpu_ctx):
+    n = 64
+    p = P.derive(GridSize=n, StepsPerTs=500, padding=2.0, VacuumGap=-1.0,
+                 S_csr=0.3)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    b = make_batch(gpu_ctx, [(p, 0, p["Ib"], 4, False)] * 3, {n: z})
+    start = b.download()
+    b.step(10)
+    after10 = b.download()
+    out = np.zeros_like(start)
+    prof = np.zeros(3 * n, np.float32)
+    fill = np.zeros(3, np.float32)
+    b.run(start, 10, out, prof, fill)
+    # restarting from the same state reproduces the trajectory (the
+    # profile of an uploaded state is recomputed from it)
+    assert rel_l1(out, after10) <= 1e-6
+    assert np.all(np.abs(fill - 1) < 1e-2)
+    assert np.all(prof.reshape(3, n).sum(1) > 0)
