@@ -254,7 +254,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=1000)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="timed steps only (for ncu): no e2e, plain loop or "
+                         "CPU legs")
     args = ap.parse_args()
+    if args.profile:
+        args.no_cpu = True
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
@@ -309,6 +314,11 @@ def main():
     ms_step = ms / args.steps
     assert ctx.device_status() == 0
     snap_low = batch.density(0)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "value": value,
+                              "ms_per_step": ms_step}), flush=True)
+        return
 
     # end to end through the C ABI with pinned host buffers
     nbytes = cells * 4

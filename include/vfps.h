@@ -143,9 +143,9 @@ VFPS_API int vfps_rotation_map_create(vfps_ps* in, vfps_ps* out,
                                       float angle, int it, int clamp,
                                       uint32_t rotmapsize, vfps_map** map);
 /* KickMap(in,out,it,clamp,axis,oclh), inc/SM/KickMap.hpp:34-38; the
- * offsets start at 0.  Clamping of kicks is not implemented by the
- * reference's CPU path (src/SM/KickMap.cpp:42-44); here it clamps to the
- * two nearest source cells, the rule of its OpenCL kernels (:80-85). */
+ * offsets start at 0.  As in the reference's CPU path, the clamp flag of a
+ * kick map is accepted and has no effect (src/SM/KickMap.cpp:42-44,
+ * :194-271); DriftMap, RFKickMap and WakePotentialMap inherit this. */
 VFPS_API int vfps_kick_map_create(vfps_ps* in, vfps_ps* out, int it,
                                   int clamp, int axis, vfps_map** map);
 /* KickMap::swapOffset (inc/SM/KickMap.hpp:54-55): count = n (x-kick) or

@@ -300,6 +300,7 @@ extern "C" int vfps_ps_create(vfps_ctx* ctx, uint32_t nb, uint32_t n,
                      "Argument \"filling\" not normalized.");
         auto p = std::make_unique<vfps_ps>();
         p->ctx = ctx;
+        p->device = ctx->device;
         p->nb = nb;
         p->n = n;
         p->charge = charge;
@@ -344,6 +345,7 @@ extern "C" int vfps_ps_copy(const vfps_ps* src, vfps_ps** ps)
     return guard(ctx, [&] {
         auto p = std::make_unique<vfps_ps>();
         p->ctx = ctx;
+        p->device = ctx->device;
         p->nb = src->nb;
         p->n = src->n;
         p->charge = src->charge;
@@ -367,8 +369,9 @@ extern "C" int vfps_ps_destroy(vfps_ps* ps)
     if (!ps) {
         return VFPS_OK;
     }
-    cudaSetDevice(ps->ctx->device);
-    cudaStreamSynchronize(ps->ctx->stream);
+    // device buffers are released with cudaFree, which waits for the
+    // device; nothing else is dereferenced (other objects may be gone)
+    cudaSetDevice(ps->device);
     delete ps;
     return VFPS_OK;
 }
@@ -601,6 +604,7 @@ std::unique_ptr<vfps_map> new_kick(vfps_ps* in, vfps_ps* out, int it,
     check_it(it);
     VFPS_REQUIRE(axis == VFPS_AXIS_X || axis == VFPS_AXIS_Y, "bad axis");
     auto m = std::make_unique<vfps_map>();
+    m->device = in->ctx->device;
     m->kind = MAP_KICK;
     m->in = in;
     m->out = out;
@@ -645,6 +649,7 @@ extern "C" int vfps_rotation_map_create(vfps_ps* in, vfps_ps* out,
                      "Clamping only supportedwith cubic interpolationand "
                      "rotmapsize > 0.");
         auto m = std::make_unique<vfps_map>();
+        m->device = in->ctx->device;
         m->kind = MAP_ROTATION;
         m->in = in;
         m->out = out;
@@ -804,6 +809,7 @@ extern "C" int vfps_fokker_planck_map_create(vfps_ps* in, vfps_ps* out,
                      "derivation must be 3 (two-sided) or 4 (cubic)");
         VFPS_REQUIRE(fptype >= 0 && fptype <= 3, "bad FPType");
         auto m = std::make_unique<vfps_map>();
+        m->device = in->ctx->device;
         m->kind = MAP_FP;
         m->in = in;
         m->out = out;
@@ -922,6 +928,7 @@ extern "C" int vfps_identity_map_create(vfps_ps* in, vfps_ps* out,
     return guard(in->ctx, [&] {
         check_pair(in, out);
         auto m = std::make_unique<vfps_map>();
+        m->device = in->ctx->device;
         m->kind = MAP_IDENTITY;
         m->in = in;
         m->out = out;
@@ -1104,8 +1111,7 @@ extern "C" int vfps_map_destroy(vfps_map* map)
     if (!map) {
         return VFPS_OK;
     }
-    cudaSetDevice(map->in->ctx->device);
-    cudaStreamSynchronize(map->in->ctx->stream);
+    cudaSetDevice(map->device);
     delete map;
     return VFPS_OK;
 }
@@ -1118,6 +1124,7 @@ std::unique_ptr<vfps_impedance> new_imp(vfps_ctx* ctx, size_t n, double fmax)
     VFPS_REQUIRE(n >= 2, "an impedance needs at least 2 frequencies");
     auto z = std::make_unique<vfps_impedance>();
     z->ctx = ctx;
+    z->device = ctx->device;
     z->nfreqs = n;
     z->f_max = fmax;
     z->z.alloc(2 * n);
@@ -1385,8 +1392,7 @@ extern "C" int vfps_impedance_destroy(vfps_impedance* imp)
     if (!imp) {
         return VFPS_OK;
     }
-    cudaSetDevice(imp->ctx->device);
-    cudaStreamSynchronize(imp->ctx->stream);
+    cudaSetDevice(imp->device);
     delete imp;
     return VFPS_OK;
 }
@@ -1407,6 +1413,7 @@ extern "C" int vfps_field_create(vfps_ps* ps, const vfps_impedance* imp,
         VFPS_REQUIRE(imp->ctx == ctx, "impedance and phase space contexts");
         auto f = std::make_unique<vfps_field>();
         f->ps = ps;
+        f->device = ctx->device;
         f->imp = imp;
         f->nmax = imp->nfreqs;
         f->spacing = spacing_bins;
@@ -1588,8 +1595,7 @@ extern "C" int vfps_field_destroy(vfps_field* field)
     if (!field) {
         return VFPS_OK;
     }
-    cudaSetDevice(field->ps->ctx->device);
-    cudaStreamSynchronize(field->ps->ctx->stream);
+    cudaSetDevice(field->device);
     delete field;
     return VFPS_OK;
 }

@@ -22,6 +22,7 @@
 // is dropped and flagged in the context's device status word.
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -541,6 +542,7 @@ __global__ void k_bgauss(const BDev* __restrict__ bd,
 // ================================================================== host
 struct vfps_batch {
     vfps_ctx* ctx = nullptr;
+    int device = 0;
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
@@ -839,6 +841,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         VFPS_REQUIRE(nb >= 1, "a batch needs at least one bunch");
         auto b = std::make_unique<vfps_batch>();
         b->ctx = ctx;
+        b->device = ctx->device;
         b->nb = nb;
         b->desc.assign(desc, desc + nb);
         b->hb.resize(nb);
@@ -1149,7 +1152,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             VFPS_CUDA(cudaStreamSynchronize(st));
         }
         VFPS_CUDA(cudaStreamSynchronize(st));
-        const int tile_cells = autotune(b.get());
+        const char* forced = std::getenv("VFPS_TILE_CELLS");
+        const int tile_cells = forced ? std::atoi(forced) : autotune(b.get());
         build_tiles(b.get(), tile_cells);
         setup_kernel(b.get());
         VFPS_CUDA(cudaStreamSynchronize(st));
@@ -1371,8 +1375,7 @@ extern "C" int vfps_batch_destroy(vfps_batch* b)
     if (!b) {
         return VFPS_OK;
     }
-    cudaSetDevice(b->ctx->device);
-    cudaStreamSynchronize(b->ctx->stream);
+    cudaSetDevice(b->device);
     destroy_graphs(b);
     delete b;
     return VFPS_OK;

@@ -74,35 +74,18 @@ __global__ void k_rotation(const float* __restrict__ in,
     out[blockIdx.z * nxy + size_t(x0) * n + y0] = value;
 }
 
-// clamp of a kick to its two nearest source cells (the rule of the
-// reference's OpenCL kick kernels, src/SM/KickMap.cpp:80-85)
-__device__ __forceinline__ float clamp2(float value, const float* line,
-                                        size_t stride, int base, int n)
-{
-    float hi = -FLT_MAX, lo = FLT_MAX;
-    bool any = false;
-    for (int k = 0; k < 2; k++) {
-        const int s = base + k;
-        if (s >= 0 && s < n) {
-            const float v = __ldg(line + size_t(s) * stride);
-            hi = fmaxf(hi, v);
-            lo = fminf(lo, v);
-            any = true;
-        }
-    }
-    return any ? fminf(fmaxf(value, lo), hi) : value;
-}
+// The reference's CPU KickMap never clamps (its interpol_clamp flag only
+// prints a notice, src/SM/KickMap.cpp:42-44), so the kick kernels follow
+// that path and take no clamp argument.
 
 // one CTA per (bunch, row x); offsets[b*n + x] in mesh units
 __global__ void k_kick_y(const float* __restrict__ in, float* __restrict__ out,
-                         const float* __restrict__ offsets, uint32_t n, int it,
-                         int clamp)
+                         const float* __restrict__ offsets, uint32_t n, int it)
 {
     const uint32_t row = blockIdx.x;
     const KickStencil s = kick_stencil(offsets[row], n, it);
     const float* src = in + size_t(row) * n;
     float* dst = out + size_t(row) * n;
-    const int h = (it - 1) / 2;
     for (uint32_t y = threadIdx.x; y < n; y += blockDim.x) {
         float value = 0.f;
         for (int j = 0; j < it; j++) {
@@ -111,17 +94,13 @@ __global__ void k_kick_y(const float* __restrict__ in, float* __restrict__ out,
                 value = fadd(value, fmul(__ldg(src + ys), s.w[j]));
             }
         }
-        if (clamp) {
-            value = clamp2(value, src, 1, int(y) + s.shift[h], int(n));
-        }
         dst[y] = value;
     }
 }
 
 // thread per cell; offsets[y] shared by all bunches
 __global__ void k_kick_x(const float* __restrict__ in, float* __restrict__ out,
-                         const float* __restrict__ offsets, uint32_t n, int it,
-                         int clamp)
+                         const float* __restrict__ offsets, uint32_t n, int it)
 {
     const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t x = blockIdx.y;
@@ -137,10 +116,6 @@ __global__ void k_kick_x(const float* __restrict__ in, float* __restrict__ out,
         if (s.valid[j] && xs >= 0 && xs < int(n)) {
             value = fadd(value, fmul(__ldg(src + size_t(xs) * n + y), s.w[j]));
         }
-    }
-    if (clamp) {
-        value = clamp2(value, src + y, n, int(x) + s.shift[(it - 1) / 2],
-                       int(n));
     }
     out[blockIdx.z * nxy + size_t(x) * n + y] = value;
 }
@@ -185,11 +160,11 @@ void launch_kick(const vfps_map* m, const float* offset)
     if (m->axis == VFPS_AXIS_Y) {
         const int threads = n >= 256 ? 256 : ((n + 31) / 32) * 32;
         k_kick_y<<<in->nb * n, threads, 0, in->ctx->stream>>>(
-            in->data.p, m->out->data.p, offset, n, m->it, m->clamp);
+            in->data.p, m->out->data.p, offset, n, m->it);
     } else {
         dim3 grid((n + 127) / 128, n, in->nb);
         k_kick_x<<<grid, 128, 0, in->ctx->stream>>>(
-            in->data.p, m->out->data.p, offset, n, m->it, m->clamp);
+            in->data.p, m->out->data.p, offset, n, m->it);
     }
     VFPS_LAUNCHED();
 }

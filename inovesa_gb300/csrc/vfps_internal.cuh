@@ -109,6 +109,7 @@ struct vfps_ctx {
 
 struct vfps_ps {
     vfps_ctx* ctx = nullptr;
+    int device = 0;                  // own copy: destroy touches nothing else
     uint32_t nb = 0, n = 0;
     double charge = 0, current = 0;
     vfps::Axis ax[2];
@@ -132,6 +133,7 @@ enum MapKind {
 
 struct vfps_map {
     MapKind kind = MAP_IDENTITY;
+    int device = 0;
     vfps_ps* in = nullptr;
     vfps_ps* out = nullptr;
     int it = 4;
@@ -157,6 +159,7 @@ struct vfps_map {
 
 struct vfps_impedance {
     vfps_ctx* ctx = nullptr;
+    int device = 0;
     size_t nfreqs = 0;
     double f_max = 0;
     vfps::DevBuf<float> z;           // interleaved re, im
@@ -164,6 +167,7 @@ struct vfps_impedance {
 
 struct vfps_field {
     vfps_ps* ps = nullptr;
+    int device = 0;
     const vfps_impedance* imp = nullptr;
     vfps::DevBuf<float> z;           // private copy of the table
     size_t nmax = 0;
