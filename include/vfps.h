@@ -339,6 +339,13 @@ VFPS_API int vfps_batch_get_wake(vfps_batch* batch, float* wake);
 /* kernel launches per solver step (for launch accounting) */
 VFPS_API int vfps_batch_info(const vfps_batch* batch, uint32_t* launches,
                              uint32_t* tile_rows);
+/* Advance every bunch by nsteps solver steps launched one kernel at a time
+ * with CUDA events between the kernels, and return the mean duration per
+ * step of each kernel in ms[3] (wake, chain-0 maps, chain-1 maps; 0 for a
+ * chain the batch does not hold).  Profiling aid (no counterpart in the
+ * reference): the state advances exactly as with vfps_batch_step. */
+VFPS_API int vfps_batch_kernel_times(vfps_batch* batch, uint32_t nsteps,
+                                     float* ms);
 VFPS_API int vfps_batch_destroy(vfps_batch* batch);
 
 #ifdef __cplusplus

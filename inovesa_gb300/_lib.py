@@ -134,6 +134,7 @@ SIGNATURES = {
     "vfps_batch_get_filling": [P, DP],
     "vfps_batch_get_wake": [P, FP],
     "vfps_batch_info": [P, U32P, U32P],
+    "vfps_batch_kernel_times": [P, u32, FP],
     "vfps_batch_destroy": [P],
 }
 

@@ -49,10 +49,11 @@ def build(force=False, verbose=False, extra_flags=()):
         return LIB
     os.makedirs(OUT, exist_ok=True)
     cc = nvcc()
-    common = ARCH + ["-lineinfo", "-O3", "-std=c++17", "--use_fast_math",
-                     "-Xcompiler", "-fPIC,-fvisibility=hidden",
+    # host code rounds like the reference's CPU build on x86-64 and aarch64:
+    # no contraction of float multiply-adds into FMA
+    common = ARCH + ["-lineinfo", "-O3", "-std=c++17",
+                     "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off",
                      "-I", os.path.join(ROOT, "include"), "-I", CSRC]
-    common = [f for f in common if f != "--use_fast_math"]
     common += list(extra_flags)
 
     def compile_one(src):

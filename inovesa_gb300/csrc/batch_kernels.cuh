@@ -1,0 +1,896 @@
+// Device side of the batched solver step (included by batch.cu only).
+//
+//  k_bwake   one CTA per bunch: the wake potential of every mesh row as
+//            the Toeplitz sum  wake[x] = s sum_m P[m] w[(x-m) mod nmax]  of
+//            the previous step's profile P (w built once per impedance in
+//            FP64), the charge integral (FP64), this step's
+//            renormalisation factor and the step counter.
+//  k_bmaps0  chain 0 (the reference's loop, src/main.cpp:1034-1044), a
+//            persistent kernel: each CTA walks its tiles (TX mesh rows of
+//            one bunch); the rows of the next tile stream into shared
+//            memory by TMA bulk copies while the current tile computes:
+//            wake and RF y-kicks fused in registers, drift x-kick as a
+//            column-wise sliding window, Fokker-Planck, new rows and their
+//            projections.
+//  k_bmaps1  chain 1 (rotation, wake y-kick, Fokker-Planck).
+#pragma once
+
+#include <cfloat>
+
+#include "vfps_internal.cuh"
+
+namespace {
+
+constexpr int THREADS = 256;
+constexpr int ROWPAD = 16;     // extra floats per rotated row (chain 1)
+constexpr int TPAD = 4;        // zero floats on each side of a t3 row
+constexpr int APAD = 32;       // zero floats left of a staged row (chain 0)
+constexpr uint64_t WAIT_NS = 1000000000ull;  // bounded TMA waits (1 s)
+
+struct BDev {
+    uint32_t n, it, chain, flags;  // flags: F_*
+    uint32_t dens_off, prof_off, tab_off, st_off;
+    uint32_t fp_off, wt_off, nmax, rot_h;
+    int32_t renorm, halo_lo, halo_hi, pad;
+    float wakescale, fillset, dq, dp;
+    float zbq, zbp, cs, sn;
+};
+
+struct Tile {
+    uint32_t bunch, x0, rows, pad;
+};
+
+// one kick stencil: tap j reads cell i + shift0 + j with weight w[j]
+// (dropped taps have weight 0)
+struct RowStencil {
+    int shift0;
+    float w[4];
+};
+
+// per staged row of chain 0: combined shift of the two y-kicks and their
+// weights
+struct RowInfo {
+    int s;      // sa + sb
+    int sb;     // shift of the second (RF) kick
+    float a[4]; // wake kick weights (times the renormalisation factor)
+    float b[4]; // RF kick weights
+};
+
+enum { F_WAKE = 1, F_FP = 2, F_CLAMP = 4 };
+enum { TAB_WS = 0, TAB_Q = 1, TAB_P = 2, TAB_COUNT = 3 };
+enum { ST_RF = 0, ST_DRIFT = 1, ST_COUNT = 2 };
+
+using namespace vfps::dev;
+
+__host__ __device__ inline size_t align16(size_t v)
+{
+    return (v + 15) & ~size_t(15);
+}
+
+// staged row of chain 0: APAD zeros, the n mesh values, APAD + 16 zeros
+// (the y-kick windows reach past the row by the kick shift)
+__host__ __device__ inline int astride0(int n) { return n + 2 * APAD + 16; }
+
+// byte offsets of the regions of k_bmaps0's dynamic shared memory; the
+// host sizes each region for the largest tile of the batch
+struct Smem0 {
+    uint32_t a[2];  // staging buffers (TMA targets)
+    uint32_t b;     // y-kicked rows [nr][n]
+    uint32_t t;     // t3 rows [rows][n + 2 TPAD]
+    uint32_t s;     // RowInfo [nr]
+    uint32_t part;  // projection partials [rows][8]
+    uint32_t bar;   // two mbarriers
+    uint32_t pads;  // per staging buffer: mesh size of its row layout and
+                    // the number of leading rows with zero pads
+    uint32_t a_floats;  // capacity of one staging buffer
+    uint32_t total;
+};
+
+__device__ __forceinline__ RowStencil make_stencil(float offset, uint32_t n,
+                                                   int it)
+{
+    const KickStencil s = kick_stencil(offset, n, it);
+    RowStencil r;
+    bool any = false;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        r.w[j] = s.valid[j] ? s.w[j] : 0.f;
+        any = any || s.valid[j];
+    }
+    r.shift0 = any ? s.shift[0] : 0;
+    return r;
+}
+
+// ----------------------------------------------------------------- wake
+__global__ void __launch_bounds__(THREADS)
+k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
+        const float* __restrict__ wt, const float* __restrict__ pin,
+        float* __restrict__ wake, float* __restrict__ factor,
+        double* __restrict__ filling, unsigned* __restrict__ counters,
+        int* __restrict__ status)
+{
+    extern __shared__ float4 wsm4[];
+    float* P = reinterpret_cast<float*>(wsm4);      // [n]
+    __shared__ double red[32];
+    const uint32_t b = blockIdx.x;
+    const BDev B = bd[b];
+    const int n = int(B.n);
+    float* W = P + n;   // W[k] = w[(k - (n-1)) mod nmax], k < 2n - 1
+    const unsigned step = *((volatile unsigned*)counters);
+    for (int i = threadIdx.x; i < n; i += THREADS) {
+        P[i] = pin[B.prof_off + i];
+    }
+    const bool has_wake = B.flags & F_WAKE;
+    if (has_wake) {
+        const int nmax = int(B.nmax);
+        const float* w = wt + B.wt_off;
+        for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
+            const int d = k - (n - 1);   // |d| < n <= nmax / 2
+            W[k] = w[d < 0 ? d + nmax : d];
+        }
+    }
+    __syncthreads();
+    // thread = (row group g of 4 consecutive rows, slice q of the m range);
+    // the four rows read W at consecutive places, so stepping m slides a
+    // register window by one: 2 shared loads per 4 multiply-adds
+    float* partial = W + 2 * n;          // [Q][n]
+    const int G = n >> 2;
+    const int Q = G >= THREADS ? 1 : THREADS / G;
+    if (has_wake) {
+        const int q = threadIdx.x / (THREADS / Q);
+        const int span = n / Q;
+        const int m0 = q * span;
+        for (int g = threadIdx.x % (THREADS / Q); g < G; g += THREADS / Q) {
+            const int x = 4 * g;
+            int bidx = x - m0 + n - 1;   // W index of (row x, m0)
+            float w0 = W[bidx], w1 = W[bidx + 1], w2 = W[bidx + 2],
+                  w3 = W[bidx + 3];
+            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+            for (int m = m0; m < m0 + span; m++) {
+                const float pm = P[m];
+                a0 = fmaf(pm, w0, a0);
+                a1 = fmaf(pm, w1, a1);
+                a2 = fmaf(pm, w2, a2);
+                a3 = fmaf(pm, w3, a3);
+                w3 = w2;
+                w2 = w1;
+                w1 = w0;
+                bidx--;
+                w0 = W[bidx > 0 ? bidx : 0];
+            }
+            float* pr = partial + size_t(q) * n + x;
+            pr[0] = a0;
+            pr[1] = a1;
+            pr[2] = a2;
+            pr[3] = a3;
+        }
+    }
+    __syncthreads();
+    for (int x = threadIdx.x; x < n; x += THREADS) {
+        float v = 0.f;
+        if (has_wake) {
+            float s = 0.f;
+            for (int q = 0; q < Q; q++) {
+                s += partial[size_t(q) * n + x];
+            }
+            v = __fmul_rn(B.wakescale, s);
+        }
+        wake[B.prof_off + x] = v;
+    }
+    // charge integral (src/PS/PhaseSpace.cpp:200-239) in FP64
+    const float* ws = tabs + B.tab_off + TAB_WS * n;
+    double a = 0;
+    for (int i = threadIdx.x; i < n; i += THREADS) {
+        a += double(P[i]) * double(ws[i]);
+    }
+    a = block_sum(a, red);
+    if (threadIdx.x == 0) {
+        filling[b] = a;
+        const bool renorm_now = B.renorm > 0
+                                && (step % unsigned(B.renorm)) == 0;
+        float f = 1.f;
+        if (renorm_now) {
+            f = B.fillset > 0 ? static_cast<float>(double(B.fillset) / a) : 0.f;
+        }
+        factor[b] = f;
+        if (B.fillset > 0 && !(a > 0)) {
+            atomicCAS(status, 0, VFPS_ERR_NUMERIC);
+        }
+        // the last CTA of the step advances the step counter
+        __threadfence();
+        const unsigned ticket = atomicAdd(counters + 1, 1u);
+        if (ticket == gridDim.x - 1) {
+            counters[1] = 0;
+            counters[0] = step + 1;
+            __threadfence();
+        }
+    }
+}
+
+// t2[i] = sum_j a_j c[AL + i + j], the first y-kick of 11 positions from
+// a window whose first input sits at c[AL]
+template <int AL>
+__device__ __forceinline__ void first_kick(const float* c, const RowInfo& ri,
+                                           float* t2)
+{
+#pragma unroll
+    for (int i = 0; i < 11; i++) {
+        float v = ri.a[0] * c[AL + i];
+        v = fmaf(ri.a[1], c[AL + i + 1], v);
+        v = fmaf(ri.a[2], c[AL + i + 2], v);
+        v = fmaf(ri.a[3], c[AL + i + 3], v);
+        t2[i] = v;
+    }
+}
+
+// per-thread column constants of the Fokker-Planck stage: the thread owns
+// the 8 energy cells y0..y0+7 of its rows (5 weights each for the offsets
+// -2..2) and their Simpson weights
+struct FpCols {
+    float f[8][5];
+    float wsr[8];
+};
+
+__device__ __forceinline__ void load_fp_cols(const BDev& B,
+                                             const float* __restrict__ fp5,
+                                             const float* __restrict__ ws,
+                                             FpCols& c)
+{
+    const int n = int(B.n);
+    const int y0 = 8 * (threadIdx.x % (n >> 3));
+    const bool has_fp = B.flags & F_FP;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        c.wsr[k] = ws[y0 + k];
+#pragma unroll
+        for (int o = 0; o < 5; o++) {
+            c.f[k][o] = has_fp ? fp5[B.fp_off + (y0 + k) * 5 + o]
+                               : (o == 2 ? 1.f : 0.f);
+        }
+    }
+}
+
+// Fokker-Planck (5 weights per column for offsets -2..2), output rows and
+// their projections.  T holds t3 rows with TPAD zeros on both sides.
+__device__ __forceinline__ void fp_and_store(
+    const float* __restrict__ T, int rows, int n, int x0, const BDev& B,
+    const FpCols& cc, float* __restrict__ dout, float* __restrict__ pout,
+    float* part)
+{
+    const int seg = n >> 3;               // threads per row
+    const int rp = THREADS / seg;         // rows in parallel
+    const int l = threadIdx.x % seg;
+    const int rl = threadIdx.x / seg;
+    const int y0 = 8 * l;
+    const int stride = n + 2 * TPAD;
+    {
+        const auto& f = cc.f;
+        const auto& wsr = cc.wsr;
+        // every lane runs the same number of iterations (the shuffles
+        // below need the whole warp); rows past the tile are predicated off
+        for (int rbase = 0; rbase < rows; rbase += rp) {
+            const int r = rbase + rl;
+            const bool valid = r < rows;
+            const float4* src = reinterpret_cast<const float4*>(
+                T + size_t(valid ? r : 0) * stride + y0);
+            float win[16];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const float4 v = src[c];
+                win[4 * c] = v.x;
+                win[4 * c + 1] = v.y;
+                win[4 * c + 2] = v.z;
+                win[4 * c + 3] = v.w;
+            }
+            float out[8];
+            float pp = 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                float v = f[k][0] * win[k + 2];
+                v = fmaf(f[k][1], win[k + 3], v);
+                v = fmaf(f[k][2], win[k + 4], v);
+                v = fmaf(f[k][3], win[k + 5], v);
+                v = fmaf(f[k][4], win[k + 6], v);
+                out[k] = v;
+                pp = fmaf(v, wsr[k], pp);
+            }
+            if (valid) {
+                float4* dst = reinterpret_cast<float4*>(
+                    dout + B.dens_off + size_t(x0 + r) * n + y0);
+                dst[0] = make_float4(out[0], out[1], out[2], out[3]);
+                dst[1] = make_float4(out[4], out[5], out[6], out[7]);
+            }
+            // reduce the row's partial sums (groups of seg lanes)
+            const int width = seg < 32 ? seg : 32;
+            for (int o = width >> 1; o > 0; o >>= 1) {
+                pp += __shfl_xor_sync(0xffffffffu, pp, o);
+            }
+            if (valid && (l & (width - 1)) == 0) {
+                part[r * 8 + (l >> 5)] = pp;
+            }
+        }
+    }
+    __syncthreads();
+    const int groups = seg < 32 ? 1 : seg / 32;
+    for (int r = threadIdx.x; r < rows; r += THREADS) {
+        float s = 0.f;
+        for (int g = 0; g < groups; g++) {
+            s += part[r * 8 + g];
+        }
+        pout[B.prof_off + x0 + r] = s;
+    }
+}
+
+// --------------------------------------------------------------- chain 0
+// Before the bulk copies of a tile land in a staging buffer: zero the
+// slots of rows off the mesh, and the pad columns of every row that does
+// not hold zero pads yet for this mesh size.  `pads` describes the buffer:
+// pads[0] = the mesh size its row layout follows, pads[1] = how many
+// leading rows have zero pads in that layout (shared memory starts with
+// arbitrary contents, and a short tail tile prepares fewer rows than a
+// later full tile reads).  Called by all threads.
+__device__ __forceinline__ void prepare_slots(const BDev& B, const Tile& t,
+                                              float* A, const int* pads)
+{
+    const int n = int(B.n);
+    const int as = astride0(n);
+    const int nr = int(t.rows) + B.halo_lo + B.halo_hi;
+    const int first = int(t.x0) - B.halo_lo;
+    const volatile int* pv = pads;
+    const int ready = pv[0] == n ? pv[1] : 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int r = warp; r < nr; r += THREADS / 32) {
+        const int x = first + r;
+        float4* row = reinterpret_cast<float4*>(A + size_t(r) * as);
+        if (unsigned(x) >= unsigned(n)) {
+            for (int j = lane; j < as / 4; j += 32) {
+                row[j] = z;
+            }
+        } else if (r >= ready) {
+            // APAD/4 float4 left of the data, (APAD + 16)/4 right of it
+            for (int j = lane; j < (2 * APAD + 16) / 4; j += 32) {
+                row[j < APAD / 4 ? j : n / 4 + j] = z;
+            }
+        }
+    }
+}
+
+// after prepare_slots (and a barrier): every row of the tile now has zero
+// pads in the layout of its mesh size (thread 0 only)
+__device__ __forceinline__ void note_slots(const BDev& B, const Tile& t,
+                                           int* pads)
+{
+    const int n = int(B.n);
+    const int nr = int(t.rows) + B.halo_lo + B.halo_hi;
+    const int ready = pads[0] == n ? pads[1] : 0;
+    pads[0] = n;
+    pads[1] = nr > ready ? nr : ready;
+}
+
+// issue the bulk copies of a tile's mesh rows (warp 0; lane 0 arms the
+// barrier with the byte count first)
+__device__ __forceinline__ void issue_tile(const BDev& B, const Tile& t,
+                                           const float* __restrict__ din,
+                                           float* A, uint64_t* bar)
+{
+    const int n = int(B.n);
+    const int as = astride0(n);
+    const int first = int(t.x0) - B.halo_lo;
+    const int lo = max(0, first);
+    const int hi = min(n, int(t.x0 + t.rows) + B.halo_hi);
+    const uint32_t row_bytes = uint32_t(n) * 4u;
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, uint32_t(hi - lo) * row_bytes);
+    }
+    __syncwarp();
+    for (int x = lo + lane; x < hi; x += 32) {
+        tma_load_1d(A + size_t(x - first) * as + APAD,
+                    din + B.dens_off + size_t(x) * n, row_bytes, bar);
+    }
+}
+
+__global__ void __launch_bounds__(THREADS, 2)
+k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
+         uint32_t ntiles, const float* __restrict__ tabs,
+         const RowStencil* __restrict__ st, const float* __restrict__ fp5,
+         const float* __restrict__ wake, const float* __restrict__ factor,
+         const float* __restrict__ din, float* __restrict__ dout,
+         float* __restrict__ pout, int* __restrict__ status, Smem0 L)
+{
+    extern __shared__ float4 smem4[];
+    char* base = reinterpret_cast<char*>(smem4);
+    float* const A0 = reinterpret_cast<float*>(base + L.a[0]);
+    float* const A1 = reinterpret_cast<float*>(base + L.a[1]);
+    float* Bs = reinterpret_cast<float*>(base + L.b);
+    float* T = reinterpret_cast<float*>(base + L.t);
+    RowInfo* S = reinterpret_cast<RowInfo*>(base + L.s);
+    float* part = reinterpret_cast<float*>(base + L.part);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
+    int* pads = reinterpret_cast<int*>(base + L.pads);   // [2][2]
+
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+        for (int i = 0; i < 4; i++) {
+            pads[i] = i & 1 ? 0 : -1;
+        }
+    }
+    __syncthreads();
+
+    // each CTA walks a contiguous chunk of the tile list (tiles of a bunch
+    // are adjacent), so per-bunch column constants stay in registers
+    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t_begin = blockIdx.x * per;
+    const uint32_t t_end = min(ntiles, t_begin + per);
+    uint32_t tid = t_begin;
+    if (tid < t_end) {
+        const Tile t = tiles[tid];
+        const BDev B = bd[t.bunch];
+        prepare_slots(B, t, A0, &pads[0]);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            note_slots(B, t, &pads[0]);
+        }
+        if (threadIdx.x < 32) {
+            issue_tile(B, t, din, A0, &bar[0]);
+        }
+    }
+    int bad = 0;
+    uint32_t cached = 0xffffffffu;   // bunch of the register caches
+    FpCols fpc;
+    RowStencil dcol;                 // drift stencil of this thread's column
+    for (uint32_t k = 0; tid < t_end; tid++, k++) {
+        const int cur = int(k & 1);
+        const Tile t = tiles[tid];
+        const BDev B = bd[t.bunch];
+        const int n = int(B.n);
+        const int x0 = int(t.x0);
+        const int rows = int(t.rows);
+        const int hlo = B.halo_lo, hhi = B.halo_hi;
+        const int nr = rows + hlo + hhi;
+        const int as = astride0(n);
+        const int it = int(B.it);
+        float* A = cur ? A1 : A0;
+        if (t.bunch != cached) {
+            cached = t.bunch;
+            load_fp_cols(B, fp5, tabs + B.tab_off + TAB_WS * n, fpc);
+            if (n <= THREADS) {
+                dcol = st[B.st_off + ST_DRIFT * n + threadIdx.x % n];
+            }
+        }
+
+        // prefetch the next tile into the other buffer: its last reader
+        // (the previous tile) finished at the barrier that ended the loop
+        const uint32_t nxt = tid + 1;
+        if (nxt < t_end) {
+            const Tile tn = tiles[nxt];
+            const BDev Bn = bd[tn.bunch];
+            prepare_slots(Bn, tn, cur ? A0 : A1, &pads[2 * (cur ^ 1)]);
+            if (threadIdx.x < 32) {
+                issue_tile(Bn, tn, din, cur ? A0 : A1, &bar[cur ^ 1]);
+            }
+        }
+
+        // per staged row: wake kick (this step) and RF kick (static)
+        {
+            const float fac = factor[t.bunch];
+            const RowStencil* rf = st + B.st_off + ST_RF * n;
+            for (int r = threadIdx.x; r < nr; r += THREADS) {
+                const int x = x0 - hlo + r;
+                RowInfo ri;
+                if (unsigned(x) < unsigned(n)) {
+                    RowStencil sa;
+                    if (B.flags & F_WAKE) {
+                        sa = make_stencil(wake[B.prof_off + x], B.n, it);
+                    } else {
+                        sa.shift0 = 0;
+                        sa.w[0] = 1.f;
+                        sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
+                    }
+                    const RowStencil sb = rf[x];
+                    ri.s = sa.shift0 + sb.shift0;
+                    ri.sb = sb.shift0;
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        // the renormalisation factor rides on the first
+                        // kick (both kicks are linear)
+                        ri.a[j] = sa.w[j] * fac;
+                        ri.b[j] = sb.w[j];
+                    }
+                } else {
+                    ri.s = 0;
+                    ri.sb = 0;
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        ri.a[j] = 0.f;
+                        ri.b[j] = 0.f;
+                    }
+                }
+                S[r] = ri;
+            }
+        }
+
+        // wait for this tile's rows (bounded: a wait that runs out flags
+        // VFPS_ERR_TIMEOUT and keeps waiting a bounded time more)
+        if (!mbar_wait_bounded(&bar[cur], (k >> 1) & 1, WAIT_NS)) {
+            bad = 1;
+            mbar_wait_bounded(&bar[cur], (k >> 1) & 1, WAIT_NS);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && nxt < t_end) {
+            const Tile tn = tiles[nxt];
+            note_slots(bd[tn.bunch], tn, &pads[2 * (cur ^ 1)]);
+        }
+
+        // both y-kicks: t2 = K_wake(t1) (zero off the mesh), t1' = K_rf(t2).
+        // The 14 inputs of 8 outputs start at mesh position y0 + s; they
+        // are read as five aligned float4 and picked at the row alignment.
+        {
+            const int seg = n >> 3;
+            const int rp = THREADS / seg;
+            const int l = threadIdx.x % seg;
+            const int rl = threadIdx.x / seg;
+            const int y0 = 8 * l;
+            for (int r = rl; r < nr; r += rp) {
+                const RowInfo ri = S[r];
+                const float* arow = A + size_t(r) * as;
+                const int start = APAD + y0 + ri.s;
+                float t2[11];
+                if (start >= 0 && (start & ~3) + 20 <= as) {
+                    const float4* src = reinterpret_cast<const float4*>(
+                        arow + (start & ~3));
+                    float c[20];
+#pragma unroll
+                    for (int q = 0; q < 5; q++) {
+                        const float4 v = src[q];
+                        c[4 * q] = v.x;
+                        c[4 * q + 1] = v.y;
+                        c[4 * q + 2] = v.z;
+                        c[4 * q + 3] = v.w;
+                    }
+                    switch (start & 3) {
+                    case 0: first_kick<0>(c, ri, t2); break;
+                    case 1: first_kick<1>(c, ri, t2); break;
+                    case 2: first_kick<2>(c, ri, t2); break;
+                    default: first_kick<3>(c, ri, t2); break;
+                    }
+                } else {
+                    // window beyond the padded row: off the mesh, zero
+                    float c[14];
+#pragma unroll
+                    for (int q = 0; q < 14; q++) {
+                        const int p = start + q;
+                        c[q] = (p >= 0 && p < as) ? arow[p] : 0.f;
+                    }
+                    first_kick<0>(c, ri, t2);
+                }
+                const int q0 = y0 + ri.sb;    // mesh position of t2[0]
+                if (q0 < 0 || q0 + 10 >= n) {
+#pragma unroll
+                    for (int i = 0; i < 11; i++) {
+                        if (unsigned(q0 + i) >= unsigned(n)) {
+                            t2[i] = 0.f;
+                        }
+                    }
+                }
+                float out[8];
+#pragma unroll
+                for (int q = 0; q < 8; q++) {
+                    float v = ri.b[0] * t2[q];
+                    v = fmaf(ri.b[1], t2[q + 1], v);
+                    v = fmaf(ri.b[2], t2[q + 2], v);
+                    v = fmaf(ri.b[3], t2[q + 3], v);
+                    out[q] = v;
+                }
+                float4* dst = reinterpret_cast<float4*>(Bs + size_t(r) * n + y0);
+                dst[0] = make_float4(out[0], out[1], out[2], out[3]);
+                dst[1] = make_float4(out[4], out[5], out[6], out[7]);
+            }
+        }
+        __syncthreads();
+
+        // drift x-kick (per-column stencil), sliding window along x; t3
+        // into T with TPAD zero columns on both sides
+        const int tstride = n + 2 * TPAD;
+        {
+            const RowStencil* dr = st + B.st_off + ST_DRIFT * n;
+            const int cols = n < THREADS ? n : THREADS;
+            const int groups = THREADS / cols;
+            const int col = threadIdx.x % cols;
+            const int g = threadIdx.x / cols;
+            const int chunk = (rows + groups - 1) / groups;
+            const int rb = g * chunk;
+            const int re = min(rows, rb + chunk);
+            for (int y = col; y < n && rb < re; y += cols) {
+                const RowStencil s = n <= THREADS ? dcol : dr[y];
+                const float* cp = Bs + y;
+                const int src = rb + hlo + s.shift0;   // staged row of tap 0
+                float w0 = cp[size_t(src) * n];
+                float w1 = cp[size_t(src + 1) * n];
+                float w2 = cp[size_t(src + 2) * n];
+                float w3 = cp[size_t(src + 3) * n];
+                for (int r = rb; r < re; r++) {
+                    float v = s.w[0] * w0;
+                    v = fmaf(s.w[1], w1, v);
+                    v = fmaf(s.w[2], w2, v);
+                    v = fmaf(s.w[3], w3, v);
+                    T[size_t(r) * tstride + TPAD + y] = v;
+                    w0 = w1;
+                    w1 = w2;
+                    w2 = w3;
+                    if (r + 1 < re) {
+                        w3 = cp[size_t(src + (r - rb) + 4) * n];
+                    }
+                }
+            }
+            for (int i = threadIdx.x; i < rows * 2 * TPAD; i += THREADS) {
+                const int r = i / (2 * TPAD), q = i % (2 * TPAD);
+                T[size_t(r) * tstride + (q < TPAD ? q : n + q)] = 0.f;
+            }
+        }
+        __syncthreads();
+
+        // Fokker-Planck, output rows, projections
+        fp_and_store(T, rows, n, x0, B, fpc, dout, pout, part);
+        __syncthreads();
+    }
+    if (bad && threadIdx.x == 0) {
+        atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
+    }
+}
+
+// --------------------------------------------------------------- chain 1
+struct Smem1 {
+    size_t a, b, s, part, total;
+};
+
+// A = staged rows [nr][n + 4] (2 zero columns each side), B = rotated rows
+// [rows][n + ROWPAD] (pre-shifted by the wake kick), S = RowStencil[rows],
+// part = [rows][8]; t3 reuses A.
+__host__ __device__ inline Smem1 smem1(int n, int nr, int rows)
+{
+    Smem1 L;
+    L.a = 0;
+    const size_t a_rows = size_t(nr) * (n + 4);
+    const size_t t_rows = size_t(rows) * (n + 2 * TPAD);
+    L.b = align16(L.a + sizeof(float) * (a_rows > t_rows ? a_rows : t_rows));
+    L.s = align16(L.b + sizeof(float) * size_t(rows) * (n + ROWPAD));
+    L.part = align16(L.s + sizeof(RowStencil) * rows);
+    L.total = align16(L.part + sizeof(float) * size_t(rows) * 8);
+    return L;
+}
+
+__global__ void __launch_bounds__(THREADS, 2)
+k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
+         const float* __restrict__ tabs, const float* __restrict__ fp5,
+         const float* __restrict__ wake, const float* __restrict__ factor,
+         const float* __restrict__ din, float* __restrict__ dout,
+         float* __restrict__ pout)
+{
+    extern __shared__ float4 smem4[];
+    char* base = reinterpret_cast<char*>(smem4);
+    const Tile t = tiles[blockIdx.x];
+    const BDev B = bd[t.bunch];
+    const int n = int(B.n);
+    const int x0 = int(t.x0);
+    const int rows = int(t.rows);
+    const int hlo = B.halo_lo, hhi = B.halo_hi;
+    const int nr = rows + hlo + hhi;
+    const Smem1 L = smem1(n, nr, rows);
+    float* A = reinterpret_cast<float*>(base + L.a);
+    float* Bs = reinterpret_cast<float*>(base + L.b);
+    RowStencil* S = reinterpret_cast<RowStencil*>(base + L.s);
+    float* part = reinterpret_cast<float*>(base + L.part);
+    const int it = int(B.it);
+    const float fac = factor[t.bunch];
+    const int astride = n + 4;
+
+    // wake kick of the tile rows
+    for (int r = threadIdx.x; r < rows; r += THREADS) {
+        RowStencil sa;
+        if (B.flags & F_WAKE) {
+            sa = make_stencil(wake[B.prof_off + x0 + r], B.n, it);
+        } else {
+            sa.shift0 = 0;
+            sa.w[0] = 1.f;
+            sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
+        }
+        S[r] = sa;
+    }
+    // stage rows x0-hlo .. x0+rows+hhi with 2 zero columns on each side
+    {
+        const float* src = din + B.dens_off;
+        const int total = nr * astride;
+        for (int i = threadIdx.x; i < total; i += THREADS) {
+            const int r = i / astride, j = i % astride;
+            const int x = x0 - hlo + r, y = j - 2;
+            float v = 0.f;
+            if (unsigned(x) < unsigned(n) && unsigned(y) < unsigned(n)) {
+                v = __ldg(src + size_t(x) * n + y) * fac;
+            }
+            A[i] = v;
+        }
+    }
+    __syncthreads();
+
+    // rotation (src/SM/RotationMap.cpp:97-260) of the tile rows; each
+    // output is written pre-shifted by its row's wake kick shift
+    {
+        const float* qv = tabs + B.tab_off + TAB_Q * n;
+        const float* pv = tabs + B.tab_off + TAB_P * n;
+        const int h = int(B.rot_h);
+        const bool clamp = B.flags & F_CLAMP;
+        const float cell0 = din[B.dens_off] * fac;
+        const int bstride = n + ROWPAD;
+        for (int i = threadIdx.x; i < rows * bstride; i += THREADS) {
+            const int r = i / bstride, j = i % bstride;
+            const int y0 = j + S[r].shift0;     // mesh column of this slot
+            float v = 0.f;
+            if (unsigned(y0) < unsigned(n)) {
+                const int xo = x0 + r;
+                const float q = qv[xo], p = pv[y0];
+                const float x1r = fadd(fdiv(fsub(fmul(B.cs, q), fmul(B.sn, p)),
+                                            B.dq), B.zbq);
+                const float y1r = fadd(fdiv(fadd(fmul(B.sn, q), fmul(B.cs, p)),
+                                            B.dp), B.zbp);
+                int x1 = 0, y1 = 0;
+                float xf, yf;
+                const bool okx = base_index(x1r, B.n, &x1, &xf);
+                const bool oky = base_index(y1r, B.n, &y1, &yf);
+                const bool ok = okx && oky;
+                if (ok) {
+                    float icq[4], icp[4];
+                    coefficients(icq, xf, it);
+                    coefficients(icp, yf, it);
+                    // staged row of tap i1: x1 + i1 - h - (x0 - hlo)
+                    const float* srow = A + size_t(x1 - h - x0 + hlo) * astride
+                                        + (y1 - h + 2);
+#pragma unroll
+                    for (int i1 = 0; i1 < 4; i1++) {
+                        if (i1 < it) {
+                            const float* rr = srow + size_t(i1) * astride;
+                            float rv = 0.f;
+#pragma unroll
+                            for (int j1 = 0; j1 < 4; j1++) {
+                                if (j1 < it) {
+                                    rv = fmaf(rr[j1], icp[j1], rv);
+                                }
+                            }
+                            v = fmaf(rv, icq[i1], v);
+                        }
+                    }
+                }
+                if (clamp) {
+                    // 2x2 nearest taps; taps off the mesh read cell (0,0)
+                    float hi = FLT_MIN, lo = FLT_MAX;
+#pragma unroll
+                    for (int i1 = 1; i1 <= 2; i1++) {
+#pragma unroll
+                        for (int j1 = 1; j1 <= 2; j1++) {
+                            const int i0 = x1 + i1 - h, j0 = y1 + j1 - h;
+                            const bool inm = ok && unsigned(i0) < unsigned(n)
+                                             && unsigned(j0) < unsigned(n);
+                            const float sv = inm
+                                ? A[size_t(i0 - x0 + hlo) * astride + j0 + 2]
+                                : cell0;
+                            hi = (hi < sv) ? sv : hi;
+                            lo = (sv < lo) ? sv : lo;
+                        }
+                    }
+                    const float tmin = (v < hi) ? v : hi;
+                    v = (tmin < lo) ? lo : tmin;
+                }
+            }
+            Bs[i] = v;
+        }
+    }
+    __syncthreads();
+
+    // wake y-kick: t3[x][y] = sum_j w_j t2[x][y + shift0 + j], the row of
+    // Bs already starts at shift0; t3 goes to A with TPAD zero columns
+    float* T = A;
+    const int tstride = n + 2 * TPAD;
+    for (int i = threadIdx.x; i < rows * tstride; i += THREADS) {
+        const int r = i / tstride, j = i % tstride;
+        const int y = j - TPAD;
+        float v = 0.f;
+        if (unsigned(y) < unsigned(n)) {
+            const RowStencil s = S[r];
+            const float* br = Bs + size_t(r) * (n + ROWPAD) + y;
+            v = s.w[0] * br[0];
+            v = fmaf(s.w[1], br[1], v);
+            v = fmaf(s.w[2], br[2], v);
+            v = fmaf(s.w[3], br[3], v);
+        }
+        T[i] = v;
+    }
+    __syncthreads();
+    FpCols fpc;
+    load_fp_cols(B, fp5, tabs + B.tab_off + TAB_WS * n, fpc);
+    fp_and_store(T, rows, n, x0, B, fpc, dout, pout, part);
+}
+
+// ------------------------------------------------------------- set-up
+// warp per packed row: profile of the current density
+__global__ void k_bproject(const BDev* __restrict__ bd,
+                           const uint32_t* __restrict__ row_bunch,
+                           const float* __restrict__ tabs,
+                           const float* __restrict__ dens,
+                           float* __restrict__ prof, uint32_t total_rows)
+{
+    const uint32_t r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= total_rows) {
+        return;
+    }
+    const BDev B = bd[row_bunch[r]];
+    const uint32_t x = r - B.prof_off;
+    if (x >= B.n) {
+        return;
+    }
+    const float* src = dens + B.dens_off + size_t(x) * B.n;
+    const float* ws = tabs + B.tab_off + TAB_WS * B.n;
+    float acc = 0.f;
+    for (uint32_t y = lane; y < B.n; y += 32) {
+        acc = fmaf(src[y], ws[y], acc);
+    }
+    acc = warp_sum_f(acc);
+    if (lane == 0) {
+        prof[r] = acc;
+    }
+}
+
+// block per bunch: filling = sum proj ws (FP64); optionally normalise
+__global__ void k_bintegrate(const BDev* __restrict__ bd,
+                             const float* __restrict__ tabs,
+                             const float* __restrict__ prof,
+                             float* __restrict__ dens,
+                             double* __restrict__ filling, int normalize)
+{
+    __shared__ double red[32];
+    __shared__ float s_f;
+    const BDev B = bd[blockIdx.x];
+    const float* ws = tabs + B.tab_off + TAB_WS * B.n;
+    double acc = 0;
+    for (uint32_t i = threadIdx.x; i < B.n; i += blockDim.x) {
+        acc += double(prof[B.prof_off + i]) * double(ws[i]);
+    }
+    acc = block_sum(acc, red);
+    if (threadIdx.x == 0) {
+        if (!normalize) {
+            filling[blockIdx.x] = acc;
+        }
+        s_f = B.fillset > 0
+                  ? static_cast<float>(double(B.fillset) / filling[blockIdx.x])
+                  : 0.f;
+    }
+    __syncthreads();
+    if (normalize) {
+        const float f = s_f;
+        float* d = dens + B.dens_off;
+        const size_t cells = size_t(B.n) * B.n;
+        for (size_t i = threadIdx.x; i < cells; i += blockDim.x) {
+            d[i] = B.fillset > 0 ? d[i] * f : 0.f;
+        }
+    }
+}
+
+__global__ void k_bgauss(const BDev* __restrict__ bd,
+                         const uint32_t* __restrict__ goff,
+                         const float* __restrict__ g, float* __restrict__ dens)
+{
+    const BDev B = bd[blockIdx.y];
+    const size_t cells = size_t(B.n) * B.n;
+    const float* gx = g + goff[blockIdx.y];
+    const float* gy = gx + B.n;
+    for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < cells;
+         i += size_t(gridDim.x) * blockDim.x) {
+        dens[B.dens_off + i] = __fmul_rn(gx[i / B.n], gy[i % B.n]);
+    }
+}
+
+}  // namespace

@@ -684,3 +684,11 @@ class BunchBatch(_Handle):
         self._check(lib().vfps_batch_info(self._h, C.byref(launches),
                                           C.byref(rows)))
         return launches.value, rows.value
+
+    def kernel_times(self, nsteps=20):
+        """Advance nsteps steps kernel by kernel; mean ms per step of the
+        wake, chain-0 and chain-1 kernels (CUDA events on the library's
+        stream)."""
+        ms = (C.c_float * 3)()
+        self._check(lib().vfps_batch_kernel_times(self._h, nsteps, ms))
+        return {"k_bwake": ms[0], "k_bmaps0": ms[1], "k_bmaps1": ms[2]}

@@ -104,6 +104,72 @@ def test_batch_matches_oracle(gpu_ctx):
     assert gpu_ctx.device_status() == 0
 
 
+def test_batch_scan_256(gpu_ctx):
+    """256^2 meshes at the two ends of the benchmark's current scan, plus a
+    few bunches in between so that tiles of several bunches share CTAs."""
+    n = 256
+    p0 = P.derive(GridSize=n, StepsPerTs=1000, padding=2.0)
+    gap = 0.006 * p0["R_bend"]
+    p = P.derive(GridSize=n, StepsPerTs=1000, padding=2.0, VacuumGap=gap)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    currents = [0.01, 0.3, 0.9, 1.5]
+    specs = [(p, 0, s * p["I_norm"], 4, False) for s in currents]
+    b = make_batch(gpu_ctx, specs, {n: z})
+    steps = 60
+    b.step(steps)
+    assert gpu_ctx.device_status() == 0
+    dens = b.download()
+    zd = z.data()
+    for i, s in enumerate(currents):
+        ref = oracle_sim(p, 0, s * p["I_norm"], zd)
+        ref.step(steps)
+        got = dens[i * n * n:(i + 1) * n * n].reshape(n, n)
+        assert rel_l1(got, ref.density(0)) <= TOL, (s, rel_l1(got, ref.density(0)))
+
+
+def test_batch_tilings_agree(gpu_ctx, monkeypatch):
+    """Every tiling of the batch gives the same bits: tiles of 4..64 rows,
+    short tail tiles, several tiles of different mesh sizes and bunches per
+    persistent CTA, both chains in one batch; two bunches against the
+    oracle."""
+    sizes = (256, 128, 256, 64)
+    z_by_n, zdata = {}, {}
+    for n in set(sizes):
+        p0 = P.derive(GridSize=n, StepsPerTs=1000, padding=2.0,
+                      VacuumGap=0.0318)
+        z_by_n[n] = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p0))
+        zdata[n] = z_by_n[n].data()
+    specs = []
+    nb = 60
+    for k in range(nb):
+        n = sizes[k % 4]
+        chain = 1 if k % 7 == 3 else 0
+        p = P.derive(GridSize=n, StepsPerTs=1000, padding=2.0,
+                     VacuumGap=0.0318, S_csr=0.05 + 1.4 * k / (nb - 1),
+                     RenormalizeCharge=(3 if k % 5 == 1 else 0))
+        specs.append((p, chain, p["Ib"], 4, False))
+    steps = 40
+    runs = []
+    for cells in ("2048", "3072", "6144", "16"):
+        monkeypatch.setenv("VFPS_TILE_CELLS", cells)
+        b = make_batch(gpu_ctx, specs, z_by_n)
+        b.step(steps)
+        assert gpu_ctx.device_status() == 0, cells
+        runs.append(b.download())
+        layout = [b.layout(i) for i in range(nb)]
+    assert np.all(np.isfinite(runs[0]))
+    for cells, r in zip(("3072", "6144", "16"), runs[1:]):
+        assert np.array_equal(r, runs[0]), cells
+    for i in (nb - 2, 3):
+        p, ch, ib, it, cl = specs[i]
+        n = p["ps_bins"]
+        ref = oracle_sim(p, ch, ib, zdata[n], it=it, clamp=cl)
+        ref.step(steps)
+        off, _ = layout[i]
+        got = runs[0][off:off + n * n].reshape(n, n)
+        assert rel_l1(got, ref.density(0)) <= TOL, i
+
+
 def test_batch_equals_plain_loop(gpu_ctx):
     """The fused kernel and the one-map-per-launch loop agree."""
     n = 128
