@@ -346,6 +346,31 @@ VFPS_API int vfps_batch_info(const vfps_batch* batch, uint32_t* launches,
  * reference): the state advances exactly as with vfps_batch_step. */
 VFPS_API int vfps_batch_kernel_times(vfps_batch* batch, uint32_t nsteps,
                                      float* ms);
+
+/* ------------------------------------------------- no-allocation helper
+ * No counterpart in the reference.  Charge integral of nb meshes [n][n]
+ * that the caller already holds in device memory (density = device
+ * pointer, e.g. vfps_ps_device_data): the Simpson x projection of every
+ * row and its Simpson integral for mesh spacing delta (the q axis of the
+ * mesh), the same numbers vfps_ps_update_x_projection followed by
+ * vfps_ps_integrate give.  integrals[nb] is host memory; the call returns
+ * after the results are there.
+ *
+ * It allocates nothing, for callers that may not allocate device memory
+ * at that point: a program that reserved its whole device budget up front
+ * and passes raw pointers into it, a pool allocator that must stay the
+ * only owner of free device memory, or a time-critical loop that cannot
+ * take the device-wide synchronisation cudaMalloc/cudaFree may cause.
+ * Its scratch is one fixed __device__ array per device: at most 262144
+ * rows (nb * n) and 4096 meshes per call, larger calls are rejected with
+ * VFPS_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * scratch address once and should come before any stream capture starts.
+ * Nothing in the scratch needs to start at zero.  Calls on one device must
+ * not overlap in time (from several host threads, or several contexts on
+ * one device): they share the scratch and would race on it. */
+VFPS_API int vfps_charge_noalloc(vfps_ctx* ctx, const float* density,
+                                 uint32_t nb, uint32_t n, float delta,
+                                 double* integrals);
 VFPS_API int vfps_batch_destroy(vfps_batch* batch);
 
 #ifdef __cplusplus

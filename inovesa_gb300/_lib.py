@@ -135,6 +135,7 @@ SIGNATURES = {
     "vfps_batch_get_wake": [P, FP],
     "vfps_batch_info": [P, U32P, U32P],
     "vfps_batch_kernel_times": [P, u32, FP],
+    "vfps_charge_noalloc": [P, P, u32, u32, flt, DP],
     "vfps_batch_destroy": [P],
 }
 
