@@ -7,7 +7,7 @@
 //            previous step's profile P (w built once per impedance in
 //            FP64), the charge integral (FP64), the renormalisation factor
 //            of this step and the step counter.
-//  k_bmaps0  chain 0 (main.cpp's loop) on a tile of TX mesh rows: wake
+//  k_bmaps0w  chain 0 (main.cpp's loop) on a tile of TX mesh rows: wake
 //            y-kick and RF y-kick fused in registers, drift x-kick,
 //            Fokker-Planck, the new rows and their projections.
 //  k_bmaps1  chain 1 (rotation, wake y-kick, Fokker-Planck).
@@ -33,18 +33,23 @@
 using vfps::DevBuf;
 
 // ================================================================== host
+enum { TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_COUNT = 3 };
+constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel
+
 struct vfps_batch {
     vfps_ctx* ctx = nullptr;
     int device = 0;
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    std::vector<Tile> htiles[2];
+    // tile lists: TL_RING (chain 0, n <= 256), TL_ROT (chain 1), TL_WIDE
+    // (chain 0, n >= 512)
+    std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
     uint32_t max_n = 0;
     DevBuf<BDev> bd;
-    DevBuf<Tile> tiles[2];
-    DevBuf<float> tabs, fp5, wt;
+    DevBuf<Tile> tiles[TL_COUNT];
+    DevBuf<float> tabs, fp5, wt, dwt;
     DevBuf<RowStencil> st;
     DevBuf<uint32_t> row_bunch;
     DevBuf<float> dens[2], prof[2];
@@ -52,9 +57,11 @@ struct vfps_batch {
     DevBuf<double> filling;
     DevBuf<unsigned> counters;
     int cur = 0;               // buffer holding the current state
-    size_t smem[2] = {0, 0};
-    Smem0 layout0{};           // shared-memory regions of k_bmaps0
-    unsigned grid0 = 0;        // persistent CTAs of k_bmaps0
+    size_t smem[TL_COUNT] = {0, 0, 0};
+    SmemR layoutR{};           // shared-memory regions of k_bmaps0
+    Smem0 layout0{};           // shared-memory regions of k_bmaps0w
+    unsigned gridR = 0;        // persistent CTAs of k_bmaps0
+    unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 1 step from buffer i
@@ -128,7 +135,7 @@ RowStencil host_stencil(float offset, uint32_t n, int it)
 }
 
 // One solver step of every bunch.  ev (optional, 4 events): recorded
-// before k_bwake and after k_bwake, k_bmaps0 and k_bmaps1.
+// before k_bwake and after k_bwake, the chain-0 kernels and k_bmaps1.
 void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
 {
     const int to = 1 - from;
@@ -147,63 +154,123 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
         b->filling.p, b->counters.p, b->ctx->d_status);
     VFPS_LAUNCHED();
     mark(1);
-    if (!b->htiles[0].empty()) {
-        k_bmaps0<<<b->grid0, THREADS, b->smem[0], st>>>(
-            b->bd.p, b->tiles[0].p,
-            static_cast<uint32_t>(b->htiles[0].size()), b->tabs.p, b->st.p,
-            b->fp5.p, b->wake.p, b->factor.p, b->dens[from].p, b->dens[to].p,
-            b->prof[to].p, b->ctx->d_status, b->layout0);
+    if (!b->htiles[TL_RING].empty()) {
+        k_bmaps0<<<b->gridR, RTHREADS, b->smem[TL_RING], st>>>(
+            b->bd.p, b->tiles[TL_RING].p,
+            static_cast<uint32_t>(b->htiles[TL_RING].size()), b->tabs.p,
+            b->st.p, b->fp5.p, b->dwt.p, b->wake.p, b->factor.p,
+            b->dens[from].p, b->dens[to].p, b->prof[to].p, b->ctx->d_status,
+            b->layoutR);
+        VFPS_LAUNCHED();
+    }
+    if (!b->htiles[TL_WIDE].empty()) {
+        k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], st>>>(
+            b->bd.p, b->tiles[TL_WIDE].p,
+            static_cast<uint32_t>(b->htiles[TL_WIDE].size()), b->tabs.p,
+            b->st.p, b->fp5.p, b->wake.p, b->factor.p, b->dens[from].p,
+            b->dens[to].p, b->prof[to].p, b->ctx->d_status, b->layout0);
         VFPS_LAUNCHED();
     }
     mark(2);
-    if (!b->htiles[1].empty()) {
-        k_bmaps1<<<static_cast<unsigned>(b->htiles[1].size()), THREADS,
-                   b->smem[1], st>>>(
-            b->bd.p, b->tiles[1].p, b->tabs.p, b->fp5.p, b->wake.p,
+    if (!b->htiles[TL_ROT].empty()) {
+        k_bmaps1<<<static_cast<unsigned>(b->htiles[TL_ROT].size()), THREADS,
+                   b->smem[TL_ROT], st>>>(
+            b->bd.p, b->tiles[TL_ROT].p, b->tabs.p, b->fp5.p, b->wake.p,
             b->factor.p, b->dens[from].p, b->dens[to].p, b->prof[to].p);
         VFPS_LAUNCHED();
     }
     mark(3);
 }
 
+// persistent grid of a kernel: as many CTAs as fit on the device with
+// `smem` bytes each, at most one per tile
+template <typename K>
+unsigned persistent_grid(vfps_batch* b, K kernel, int threads, size_t smem,
+                         size_t ntiles)
+{
+    int per_sm = 0;
+    if (smem <= 227 * 1024
+        && cudaFuncSetAttribute(kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                static_cast<int>(smem)) == cudaSuccess
+        && cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+               &per_sm, kernel, threads, smem) == cudaSuccess) {
+        per_sm = std::max(per_sm, 1);
+    } else {
+        per_sm = 1;
+    }
+    return static_cast<unsigned>(
+        std::min<size_t>(ntiles, size_t(per_sm) * b->ctx->sm_count));
+}
+
 void build_tiles(vfps_batch* b, int tile_cells)
 {
-    for (int c = 0; c < 2; c++) {
+    for (int c = 0; c < TL_COUNT; c++) {
         b->htiles[c].clear();
         b->smem[c] = 0;
     }
     int max_rows = 0;
-    // chain 0 regions sized for the largest tile of the batch
+    // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
+    int ring_rows = 0, ring_n = 0;
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
+        const int c = B.chain == 1 ? TL_ROT
+                      : (n <= RING_MAX_N ? TL_RING : TL_WIDE);
         int tx = std::max(4, tile_cells / n);
+        if (c == TL_RING) {
+            // the ring holds two tiles with their halos: at most 32 staged
+            // rows per tile keeps it at 64 slots
+            tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
+        }
         tx = std::min(tx, n);
         max_rows = std::max(max_rows, tx);
-        const int c = int(B.chain);
         for (int x0 = 0; x0 < n; x0 += tx) {
             const int rows = std::min(tx, n - x0);
             b->htiles[c].push_back({i, uint32_t(x0), uint32_t(rows), 0});
         }
         const int nr = tx + B.halo_lo + B.halo_hi;
-        if (c == 0) {
+        if (c == TL_RING) {
+            ring_rows = std::max(ring_rows, nr);
+            ring_n = std::max(ring_n, n);
+        } else if (c == TL_WIDE) {
             a_floats = std::max(a_floats, size_t(nr) * astride0(n));
             b_floats = std::max(b_floats, size_t(nr) * n);
             t_floats = std::max(t_floats, size_t(tx) * (n + 2 * TPAD));
             s_rows = std::max(s_rows, size_t(nr));
             p_rows = std::max(p_rows, size_t(tx));
         } else {
-            b->smem[1] = std::max(b->smem[1], smem1(n, nr, tx).total);
+            b->smem[TL_ROT] = std::max(b->smem[TL_ROT],
+                                       smem1(n, nr, tx).total);
         }
     }
-    if (!b->htiles[0].empty()) {
+    size_t o = 0;
+    auto take = [&](uint32_t* at, size_t bytes) {
+        *at = static_cast<uint32_t>(o);
+        o = align16(o + bytes);
+    };
+    if (!b->htiles[TL_RING].empty()) {
+        // the ring holds the staged rows of two tiles with their halos
+        SmemR& L = b->layoutR;
+        int rb = 1;
+        while (rb < 2 * ring_rows) {
+            rb *= 2;
+        }
+        L.rb = static_cast<uint32_t>(rb);
+        L.rs = static_cast<uint32_t>(astride0(ring_n));
+        o = 0;
+        take(&L.ring, size_t(rb) * L.rs * 4);
+        take(&L.s, size_t(ring_rows) * sizeof(RowInfo));
+        take(&L.bar, 2 * sizeof(uint64_t));
+        L.total = static_cast<uint32_t>(o);
+        b->smem[TL_RING] = o;
+        b->gridR = persistent_grid(b, k_bmaps0, RTHREADS, o,
+                                   b->htiles[TL_RING].size());
+    }
+    if (!b->htiles[TL_WIDE].empty()) {
         Smem0& L = b->layout0;
-        size_t o = 0;
-        auto take = [&](uint32_t* at, size_t bytes) {
-            *at = static_cast<uint32_t>(o);
-            o = align16(o + bytes);
-        };
+        o = 0;
         take(&L.a[0], a_floats * 4);
         take(&L.a[1], a_floats * 4);
         take(&L.b, b_floats * 4);
@@ -214,22 +281,9 @@ void build_tiles(vfps_batch* b, int tile_cells)
         take(&L.pads, 4 * sizeof(int));
         L.a_floats = static_cast<uint32_t>(a_floats);
         L.total = static_cast<uint32_t>(o);
-        b->smem[0] = o;
-        // persistent grid: as many CTAs as fit on the device, at most one
-        // per tile
-        int per_sm = 0;
-        if (o <= 227 * 1024
-            && cudaFuncSetAttribute(k_bmaps0,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    static_cast<int>(o)) == cudaSuccess
-            && cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &per_sm, k_bmaps0, THREADS, o) == cudaSuccess) {
-            per_sm = std::max(per_sm, 1);
-        } else {
-            per_sm = 1;
-        }
-        b->grid0 = static_cast<unsigned>(std::min<size_t>(
-            b->htiles[0].size(), size_t(per_sm) * b->ctx->sm_count));
+        b->smem[TL_WIDE] = o;
+        b->grid0 = persistent_grid(b, k_bmaps0w, THREADS, o,
+                                   b->htiles[TL_WIDE].size());
     }
     b->tile_cells = tile_cells;
     b->tile_rows = max_rows;
@@ -237,7 +291,12 @@ void build_tiles(vfps_batch* b, int tile_cells)
 
 bool tiles_fit(const vfps_batch* b)
 {
-    return b->smem[0] <= 227 * 1024 && b->smem[1] <= 227 * 1024;
+    for (int c = 0; c < TL_COUNT; c++) {
+        if (b->smem[c] > 227 * 1024) {
+            return false;
+        }
+    }
+    return true;
 }
 
 void upload_tiles(vfps_batch* b)
@@ -247,12 +306,16 @@ void upload_tiles(vfps_batch* b)
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
-                                       b->smem[0], 1))));
+                                       b->smem[TL_RING], 1))));
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0w,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_WIDE], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps1,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
-                                       b->smem[1], 1))));
-    for (int c = 0; c < 2; c++) {
+                                       b->smem[TL_ROT], 1))));
+    for (int c = 0; c < TL_COUNT; c++) {
         b->tiles[c].alloc(std::max<size_t>(b->htiles[c].size(), 1));
         if (!b->htiles[c].empty()) {
             VFPS_CUDA(cudaMemcpy(b->tiles[c].p, b->htiles[c].data(),
@@ -534,7 +597,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         b->nb = nb;
         b->desc.assign(desc, desc + nb);
         b->hb.resize(nb);
-        std::vector<float> tabs, fp5, wt, gauss;
+        std::vector<float> tabs, fp5, wt, gauss, dwt;
         std::vector<RowStencil> sts;
         std::vector<uint32_t> row_bunch, goff;
         std::vector<uint32_t> wt_off(nimp, 0xffffffffu);
@@ -648,6 +711,21 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             }
             sts.insert(sts.end(), rf.begin(), rf.end());
             sts.insert(sts.end(), dr.begin(), dr.end());
+            if (d.chain == 0) {
+                // drift stencils as planes for 16-byte loads: w[j][y] for
+                // j < 4, then shift0[y] (int bits)
+                B.dw_off = static_cast<uint32_t>(dwt.size());
+                for (int j = 0; j < 4; j++) {
+                    for (uint32_t y = 0; y < n; y++) {
+                        dwt.push_back(dr[y].w[j]);
+                    }
+                }
+                for (uint32_t y = 0; y < n; y++) {
+                    float f;
+                    std::memcpy(&f, &dr[y].shift0, sizeof(f));
+                    dwt.push_back(f);
+                }
+            }
             if (d.e1 > 0) {
                 B.flags |= F_FP;
                 const auto w5 = fp_weights(ay, float(d.e1), d.fptype,
@@ -708,6 +786,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         put(b->tabs, tabs);
         put(b->st, sts);
         put(b->fp5, fp5);
+        put(b->dwt, dwt);
         b->wt.alloc(std::max<size_t>(wt.size(), 1));
         for (uint32_t k = 0; k < nimp; k++) {
             if (wt_off[k] != 0xffffffffu) {
@@ -978,8 +1057,10 @@ extern "C" int vfps_batch_info(const vfps_batch* b, uint32_t* launches,
     }
     if (launches) {
         // wake kernel + one map kernel per chain present
-        *launches = 1 + (b->htiles[0].empty() ? 0 : 1)
-                    + (b->htiles[1].empty() ? 0 : 1);
+        *launches = 1;
+        for (int c = 0; c < TL_COUNT; c++) {
+            *launches += b->htiles[c].empty() ? 0 : 1;
+        }
     }
     if (tile_rows) {
         *tile_rows = static_cast<uint32_t>(b->tile_rows);

@@ -5,13 +5,17 @@
 //            the previous step's profile P (w built once per impedance in
 //            FP64), the charge integral (FP64), this step's
 //            renormalisation factor and the step counter.
-//  k_bmaps0  chain 0 (the reference's loop, src/main.cpp:1034-1044), a
-//            persistent kernel: each CTA walks its tiles (TX mesh rows of
-//            one bunch); the rows of the next tile stream into shared
-//            memory by TMA bulk copies while the current tile computes:
-//            wake and RF y-kicks fused in registers, drift x-kick as a
-//            column-wise sliding window, Fokker-Planck, new rows and their
-//            projections.
+//  k_bmaps0  chain 0 (the reference's loop, src/main.cpp:1034-1044) for
+//            meshes up to 256 rows: a persistent kernel whose CTAs walk
+//            consecutive tiles of mesh rows through a ring of staged rows
+//            in shared memory (TMA bulk copies one tile ahead); rows are
+//            y-kicked in place once, the drift x-kick and Fokker-Planck
+//            stage reads them from the ring, new rows and projections go
+//            straight to HBM.  One CTA barrier per tile.
+//  k_bmaps0w  chain 0 for wider meshes: tiles staged with their halo in
+//            double-buffered shared memory (TMA bulk copies), y-kicks fused
+//            in registers, drift x-kick as a column-wise sliding window,
+//            Fokker-Planck, new rows and their projections.
 //  k_bmaps1  chain 1 (rotation, wake y-kick, Fokker-Planck).
 #pragma once
 
@@ -31,7 +35,8 @@ struct BDev {
     uint32_t n, it, chain, flags;  // flags: F_*
     uint32_t dens_off, prof_off, tab_off, st_off;
     uint32_t fp_off, wt_off, nmax, rot_h;
-    int32_t renorm, halo_lo, halo_hi, pad;
+    int32_t renorm, halo_lo, halo_hi;
+    uint32_t dw_off;               // drift planes (chain 0, n <= 256)
     float wakescale, fillset, dq, dp;
     float zbq, zbp, cs, sn;
 };
@@ -71,7 +76,7 @@ __host__ __device__ inline size_t align16(size_t v)
 // (the y-kick windows reach past the row by the kick shift)
 __host__ __device__ inline int astride0(int n) { return n + 2 * APAD + 16; }
 
-// byte offsets of the regions of k_bmaps0's dynamic shared memory; the
+// byte offsets of the regions of k_bmaps0w's dynamic shared memory; the
 // host sizes each region for the largest tile of the batch
 struct Smem0 {
     uint32_t a[2];  // staging buffers (TMA targets)
@@ -393,7 +398,7 @@ __device__ __forceinline__ void issue_tile(const BDev& B, const Tile& t,
 }
 
 __global__ void __launch_bounds__(THREADS, 2)
-k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
+k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          uint32_t ntiles, const float* __restrict__ tabs,
          const RowStencil* __restrict__ st, const float* __restrict__ fp5,
          const float* __restrict__ wake, const float* __restrict__ factor,
@@ -637,6 +642,504 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         // Fokker-Planck, output rows, projections
         fp_and_store(T, rows, n, x0, B, fpc, dout, pout, part);
         __syncthreads();
+    }
+    if (bad && threadIdx.x == 0) {
+        atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
+    }
+}
+
+// ------------------------------------------- chain 0, meshes up to 256
+// Lane mapping of the row stages: the n cells of a row are served by
+// seg = n/8 consecutive lanes of one warp; lane l owns the two groups of 4
+// columns that start at 4l and n/2 + 4l, so that the lanes of a row read
+// and write consecutive 16-byte words (no shared-memory bank conflicts).
+// Staged rows live in a ring of RB slots (a power of two) of RS floats:
+// APAD zeros, the row, zeros; a tile's rows get the slots after the rows
+// staged before it, and consecutive tiles of a bunch share their halo rows.
+constexpr int RTHREADS = 128;
+
+struct SmemR {
+    uint32_t ring;  // RB slots of RS floats
+    uint32_t s;     // RowInfo of the rows staged for one tile
+    uint32_t bar;   // two mbarriers
+    uint32_t rb;    // ring slots (power of two)
+    uint32_t rs;    // floats per slot
+    uint32_t total;
+};
+
+// Fokker-Planck weights (offsets -2..2) of the 8 columns a lane owns,
+// [group * 4 + column], and the Simpson step h03 = delta/3 (the weights are
+// h03 at both ends of the row, else 4 h03 at odd and 2 h03 at even columns)
+struct FpCols2 {
+    float f[8][5];
+    float h03;
+};
+
+__device__ __forceinline__ int lane_col(int n, int l, int k)
+{
+    return (k >> 2) * (n >> 1) + 4 * l + (k & 3);
+}
+
+__device__ __forceinline__ void load_fp_cols2(const BDev& B,
+                                              const float* __restrict__ fp5,
+                                              const float* __restrict__ ws,
+                                              FpCols2& c)
+{
+    const int n = int(B.n);
+    const int l = threadIdx.x % (n >> 3);
+    const bool has_fp = B.flags & F_FP;
+    c.h03 = ws[0];
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int y = lane_col(n, l, k);
+#pragma unroll
+        for (int o = 0; o < 5; o++) {
+            c.f[k][o] = has_fp ? fp5[B.fp_off + y * 5 + o]
+                               : (o == 2 ? 1.f : 0.f);
+        }
+    }
+}
+
+// wake (times the renormalisation factor) and RF y-kick stencils of mesh
+// row x
+__device__ __forceinline__ RowInfo row_info(const BDev& B, int x,
+                                            const float* __restrict__ wake,
+                                            const RowStencil* __restrict__ rf,
+                                            float fac)
+{
+    RowStencil sa;
+    if (B.flags & F_WAKE) {
+        sa = make_stencil(wake[B.prof_off + x], B.n, int(B.it));
+    } else {
+        sa.shift0 = 0;
+        sa.w[0] = 1.f;
+        sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
+    }
+    const RowStencil sb = rf[x];
+    RowInfo ri;
+    ri.s = sa.shift0 + sb.shift0;
+    ri.sb = sb.shift0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        // the renormalisation factor rides on the first kick (both kicks
+        // are linear)
+        ri.a[j] = sa.w[j] * fac;
+        ri.b[j] = sb.w[j];
+    }
+    return ri;
+}
+
+// t2[i] = sum_j a_j c[AL + i + j] for the 7 positions the second kick of
+// 4 cells reads
+template <int AL>
+__device__ __forceinline__ void kick7(const float* c, const RowInfo& ri,
+                                      float* t2)
+{
+#pragma unroll
+    for (int i = 0; i < 7; i++) {
+        float v = ri.a[0] * c[AL + i];
+        v = fmaf(ri.a[1], c[AL + i + 1], v);
+        v = fmaf(ri.a[2], c[AL + i + 2], v);
+        v = fmaf(ri.a[3], c[AL + i + 3], v);
+        t2[i] = v;
+    }
+}
+
+// Both y-kicks of the 4 cells y..y+3 of a staged row (mesh value of
+// column y at row[APAD + y]): t2 = K_wake(t1), zero off the mesh, then
+// K_rf(t2).  The 10 inputs start at mesh column y + s.
+__device__ __forceinline__ float4 ykick4(const float* row, int as, int n,
+                                         int y, const RowInfo& ri)
+{
+    const int start = APAD + y + ri.s;
+    float t2[7];
+    if (start >= 0 && (start & ~3) + 16 <= as) {
+        const float4* src = reinterpret_cast<const float4*>(row + (start & ~3));
+        float c[16];
+        const float4 v0 = src[0], v1 = src[1], v2 = src[2];
+        c[0] = v0.x; c[1] = v0.y; c[2] = v0.z; c[3] = v0.w;
+        c[4] = v1.x; c[5] = v1.y; c[6] = v1.z; c[7] = v1.w;
+        c[8] = v2.x; c[9] = v2.y; c[10] = v2.z; c[11] = v2.w;
+        switch (start & 3) {
+        case 0: kick7<0>(c, ri, t2); break;
+        case 1: kick7<1>(c, ri, t2); break;
+        case 2: kick7<2>(c, ri, t2); break;
+        default: {
+            const float4 v3 = src[3];
+            c[12] = v3.x; c[13] = v3.y; c[14] = v3.z; c[15] = v3.w;
+            kick7<3>(c, ri, t2);
+            break;
+        }
+        }
+    } else {
+        // window beyond the padded row: those cells are off the mesh
+        float c[10];
+#pragma unroll
+        for (int q = 0; q < 10; q++) {
+            const int p = start + q;
+            c[q] = (p >= 0 && p < as) ? row[p] : 0.f;
+        }
+        kick7<0>(c, ri, t2);
+    }
+    const int q0 = y + ri.sb;    // mesh column of t2[0]
+    if (q0 < 0 || q0 + 6 >= n) {
+#pragma unroll
+        for (int i = 0; i < 7; i++) {
+            if (unsigned(q0 + i) >= unsigned(n)) {
+                t2[i] = 0.f;
+            }
+        }
+    }
+    float o[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float v = ri.b[0] * t2[q];
+        v = fmaf(ri.b[1], t2[q + 1], v);
+        v = fmaf(ri.b[2], t2[q + 2], v);
+        v = fmaf(ri.b[3], t2[q + 3], v);
+        o[q] = v;
+    }
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// ring slot of mesh row x of the current segment
+struct RingMap {
+    int xref, pref;
+    __device__ __forceinline__ int slot(int x, int rb) const
+    {
+        return (x - xref + pref) & (rb - 1);
+    }
+};
+
+// bulk copies of the mesh rows among [lo, hi) into their slots (warp 0;
+// lane 0 arms the barrier with the byte count first)
+__device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
+                                           const RingMap& m, float* ring,
+                                           int rb, int rs,
+                                           const float* __restrict__ din,
+                                           uint64_t* bar)
+{
+    const int n = int(B.n);
+    const int a = max(lo, 0), e = min(hi, n);
+    const uint32_t row_bytes = uint32_t(n) * 4u;
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, uint32_t(e - a) * row_bytes);
+    }
+    __syncwarp();
+    for (int x = a + lane; x < e; x += 32) {
+        tma_load_1d(ring + size_t(m.slot(x, rb)) * rs + APAD,
+                    din + B.dens_off + size_t(x) * n, row_bytes, bar);
+    }
+}
+
+// Drift x-kick of two output rows and 4 columns from the ring: tap j of
+// output row X reads staged row X + shift + j.  The 5 staged rows stream
+// through registers (tap j of the first row and tap j - 1 of the second
+// share row j).
+__device__ __forceinline__ void drift2(const float* ring, const RingMap& m,
+                                       int rb, int rs, int X0, int y,
+                                       const float* __restrict__ W, int n,
+                                       float* d0, float* d1)
+{
+    const int4 sh = __ldg(reinterpret_cast<const int4*>(W + 4 * n + y));
+    if (sh.x == sh.y && sh.y == sh.z && sh.z == sh.w) {
+        float4 wp = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            const float4 v = *reinterpret_cast<const float4*>(
+                ring + size_t(m.slot(X0 + sh.x + j, rb)) * rs + APAD + y);
+            const float vv[4] = {v.x, v.y, v.z, v.w};
+            float4 wj = wp;
+            if (j < 4) {
+                wj = __ldg(reinterpret_cast<const float4*>(W + j * n + y));
+            }
+            const float wc[4] = {wj.x, wj.y, wj.z, wj.w};
+            const float pc[4] = {wp.x, wp.y, wp.z, wp.w};
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                if (j == 0) {
+                    d0[c] = wc[c] * vv[c];
+                } else if (j < 4) {
+                    d0[c] = fmaf(wc[c], vv[c], d0[c]);
+                }
+                if (j == 1) {
+                    d1[c] = pc[c] * vv[c];
+                } else if (j > 1) {
+                    d1[c] = fmaf(pc[c], vv[c], d1[c]);
+                }
+            }
+            wp = wj;
+        }
+    } else {
+        // a shift boundary inside the 4 columns: column by column
+        const int shv[4] = {sh.x, sh.y, sh.z, sh.w};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float q[5];
+#pragma unroll
+            for (int j = 0; j < 5; j++) {
+                q[j] = ring[size_t(m.slot(X0 + shv[c] + j, rb)) * rs + APAD
+                            + y + c];
+            }
+            const float w0 = W[y + c], w1 = W[n + y + c],
+                        w2 = W[2 * n + y + c], w3 = W[3 * n + y + c];
+            float v = w0 * q[0];
+            v = fmaf(w1, q[1], v);
+            v = fmaf(w2, q[2], v);
+            v = fmaf(w3, q[3], v);
+            d0[c] = v;
+            float u = w0 * q[1];
+            u = fmaf(w1, q[2], u);
+            u = fmaf(w2, q[3], u);
+            u = fmaf(w3, q[4], u);
+            d1[c] = u;
+        }
+    }
+}
+
+// Fokker-Planck of one row's 8 lane cells from their drift values d[8]
+// (group A then group B) and the neighbours' (shuffles within the row's
+// seg lanes); stores the row and returns its projection partial
+__device__ __forceinline__ float fp_row(const float* d, int l, int seg,
+                                        const FpCols2& cc, float* dst_a,
+                                        float* dst_b, bool valid)
+{
+    const int lp = (l + 1) & (seg - 1), lm = (l + seg - 1) & (seg - 1);
+    const float rA0 = __shfl_sync(0xffffffffu, d[0], lp, seg);
+    const float rA1 = __shfl_sync(0xffffffffu, d[1], lp, seg);
+    const float rB0 = __shfl_sync(0xffffffffu, d[4], lp, seg);
+    const float rB1 = __shfl_sync(0xffffffffu, d[5], lp, seg);
+    const float lA2 = __shfl_sync(0xffffffffu, d[2], lm, seg);
+    const float lA3 = __shfl_sync(0xffffffffu, d[3], lm, seg);
+    const float lB2 = __shfl_sync(0xffffffffu, d[6], lm, seg);
+    const float lB3 = __shfl_sync(0xffffffffu, d[7], lm, seg);
+    const bool first = l == 0, last = l == seg - 1;
+    // columns -2..5 around each group
+    const float wa[8] = {first ? 0.f : lA2, first ? 0.f : lA3, d[0], d[1],
+                         d[2], d[3], last ? rB0 : rA0, last ? rB1 : rA1};
+    const float wb[8] = {first ? lA2 : lB2, first ? lA3 : lB3, d[4], d[5],
+                         d[6], d[7], last ? 0.f : rB0, last ? 0.f : rB1};
+    float out[8];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float v = cc.f[c][0] * wa[c];
+        v = fmaf(cc.f[c][1], wa[c + 1], v);
+        v = fmaf(cc.f[c][2], wa[c + 2], v);
+        v = fmaf(cc.f[c][3], wa[c + 3], v);
+        v = fmaf(cc.f[c][4], wa[c + 4], v);
+        out[c] = v;
+        float u = cc.f[4 + c][0] * wb[c];
+        u = fmaf(cc.f[4 + c][1], wb[c + 1], u);
+        u = fmaf(cc.f[4 + c][2], wb[c + 2], u);
+        u = fmaf(cc.f[4 + c][3], wb[c + 3], u);
+        u = fmaf(cc.f[4 + c][4], wb[c + 4], u);
+        out[4 + c] = u;
+    }
+    if (valid) {
+        *reinterpret_cast<float4*>(dst_a) =
+            make_float4(out[0], out[1], out[2], out[3]);
+        *reinterpret_cast<float4*>(dst_b) =
+            make_float4(out[4], out[5], out[6], out[7]);
+    }
+    // Simpson-weighted partial sum: lane columns alternate even, odd, so
+    // the weights are 2 h03, 4 h03 except for columns 0 and n - 1 (h03)
+    const float pe = (out[0] + out[2]) + (out[4] + out[6]);
+    const float po = (out[1] + out[3]) + (out[5] + out[7]);
+    float pp = fmaf(4.f, po, 2.f * pe);
+    if (first) {
+        pp -= out[0];
+    }
+    if (last) {
+        pp = fmaf(-3.f, out[7], pp);
+    }
+    return cc.h03 * pp;
+}
+
+__global__ void __launch_bounds__(RTHREADS, 4)
+k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
+         uint32_t ntiles, const float* __restrict__ tabs,
+         const RowStencil* __restrict__ st, const float* __restrict__ fp5,
+         const float* __restrict__ dwt, const float* __restrict__ wake,
+         const float* __restrict__ factor, const float* __restrict__ din,
+         float* __restrict__ dout, float* __restrict__ pout,
+         int* __restrict__ status, SmemR L)
+{
+    extern __shared__ float4 smem4[];
+    char* base = reinterpret_cast<char*>(smem4);
+    float* ring = reinterpret_cast<float*>(base + L.ring);
+    RowInfo* S = reinterpret_cast<RowInfo*>(base + L.s);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
+    const int rb = int(L.rb), rs = int(L.rs);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // the ring starts zero: slots are written only in [APAD, APAD + n + 48)
+    {
+        float4* r4 = reinterpret_cast<float4*>(ring);
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = threadIdx.x; i < rb * rs / 4; i += RTHREADS) {
+            r4[i] = z;
+        }
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    fence_proxy_async();
+    __syncthreads();
+
+    // each CTA walks a contiguous chunk of the tile list: tiles of a bunch
+    // are adjacent and in row order, so consecutive tiles share halo rows
+    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+    const uint32_t t_begin = blockIdx.x * per;
+    const uint32_t t_end = min(ntiles, t_begin + per);
+
+    // ring state of the current and of the next tile: slot mapping and the
+    // new rows [lo, hi) staged for it
+    RingMap mc{0, 0}, mn{0, 0};
+    int lo_c = 0, hi_c = 0, lo_n = 0, hi_n = 0;
+    int front = 0;   // ring position after the last staged row
+    if (t_begin < t_end) {
+        const Tile t = tiles[t_begin];
+        const BDev B = bd[t.bunch];
+        lo_c = int(t.x0) - B.halo_lo;
+        hi_c = int(t.x0 + t.rows) + B.halo_hi;
+        mc = RingMap{lo_c, 0};
+        front = hi_c - lo_c;
+        if (warp == 0) {
+            issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, &bar[0]);
+        }
+    }
+    int bad = 0;
+    uint32_t cached = 0xffffffffu;
+    FpCols2 fpc;
+    for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
+        const Tile t = tiles[tid];
+        const BDev B = bd[t.bunch];
+        const int n = int(B.n);
+        const int x0 = int(t.x0);
+        const int rows = int(t.rows);
+        const int seg = n >> 3;
+        const int l = threadIdx.x % seg;
+        const int rl = threadIdx.x / seg;
+        const int rp = RTHREADS / seg;
+        const int as = astride0(n);
+        if (t.bunch != cached) {
+            cached = t.bunch;
+            load_fp_cols2(B, fp5, tabs + B.tab_off + TAB_WS * n, fpc);
+        }
+
+        // stage 1: RowInfo of the new rows this warp owns (lane q of the
+        // warp takes the q-th of them), then their y-kicks in place
+        {
+            const int m = hi_c - lo_c;
+            const int rpw = 32 / seg;          // rows side by side in a warp
+            const float fac = factor[t.bunch];
+            const RowStencil* rf = st + B.st_off + ST_RF * n;
+            for (int q = lane; ; q += 32) {
+                const int i = warp * rpw + q % rpw + (q / rpw) * rp;
+                if (i >= m) {
+                    break;
+                }
+                const int x = lo_c + i;
+                if (unsigned(x) < unsigned(n)) {
+                    S[i] = row_info(B, x, wake, rf, fac);
+                }
+            }
+            __syncwarp();
+            if (!mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, WAIT_NS)) {
+                bad = 1;
+                mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, WAIT_NS);
+            }
+            // lanes of one row: a segment of seg lanes of this warp
+            const unsigned rmask = seg == 32 ? 0xffffffffu
+                : (((1u << seg) - 1u) << ((lane / seg) * seg));
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int i = rl; i < m; i += rp) {
+                const int x = lo_c + i;
+                float* row = ring + size_t(mc.slot(x, rb)) * rs;
+                // zeros right of the row (the slot may have held a longer
+                // row of another bunch)
+                for (int j = l; j < 12; j += seg) {
+                    reinterpret_cast<float4*>(row + APAD + n)[j] = z;
+                }
+                if (unsigned(x) < unsigned(n)) {
+                    __syncwarp(rmask);
+                    const RowInfo ri = S[i];
+                    const int ya = 4 * l, yb = (n >> 1) + 4 * l;
+                    const float4 oa = ykick4(row, as, n, ya, ri);
+                    const float4 ob = ykick4(row, as, n, yb, ri);
+                    __syncwarp(rmask);
+                    *reinterpret_cast<float4*>(row + APAD + ya) = oa;
+                    *reinterpret_cast<float4*>(row + APAD + yb) = ob;
+                } else {
+                    reinterpret_cast<float4*>(row + APAD)[l] = z;
+                    reinterpret_cast<float4*>(row + APAD + (n >> 1))[l] = z;
+                }
+            }
+        }
+        // the in-place writes precede later bulk copies into these slots
+        fence_proxy_async();
+        __syncthreads();
+
+        // stage the next tile's new rows: their slots hold no row that this
+        // tile still reads (the ring holds two tiles with their halos)
+        if (tid + 1 < t_end) {
+            const Tile tn = tiles[tid + 1];
+            const BDev Bn = bd[tn.bunch];
+            const bool cont = tn.bunch == t.bunch
+                              && int(tn.x0) == x0 + rows;
+            hi_n = int(tn.x0 + tn.rows) + Bn.halo_hi;
+            if (cont) {
+                mn = mc;
+                lo_n = hi_c;
+            } else {
+                lo_n = int(tn.x0) - Bn.halo_lo;
+                mn = RingMap{lo_n, front};
+            }
+            front = hi_n - mn.xref + mn.pref;
+            if (warp == 0) {
+                issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din,
+                           &bar[(k + 1) & 1]);
+            }
+        }
+
+        // drift x-kick, Fokker-Planck, output rows and projections, two
+        // rows per lane segment
+        {
+            const float* W = dwt + B.dw_off;
+            const int hw = seg >> 1;
+            for (int rbase = 0; rbase < rows; rbase += 2 * rp) {
+                const int r0 = rbase + 2 * rl;
+                const bool v0 = r0 < rows, v1 = r0 + 1 < rows;
+                const int X0 = x0 + (v0 ? r0 : 0);
+                float d0[8], d1[8];
+                drift2(ring, mc, rb, rs, X0, 4 * l, W, n, d0, d1);
+                drift2(ring, mc, rb, rs, X0, (n >> 1) + 4 * l, W, n, d0 + 4,
+                       d1 + 4);
+                float* o0 = dout + B.dens_off + size_t(X0) * n;
+                const float pa = fp_row(d0, l, seg, fpc, o0 + 4 * l,
+                                        o0 + (n >> 1) + 4 * l, v0);
+                const float pb = fp_row(d1, l, seg, fpc, o0 + n + 4 * l,
+                                        o0 + n + (n >> 1) + 4 * l, v1);
+                // row sums of both rows in one butterfly: the lower half of
+                // the segment sums row r0, the upper half row r0 + 1
+                const bool up = (l & hw) != 0;
+                float v = (up ? pb : pa)
+                          + __shfl_xor_sync(0xffffffffu, up ? pa : pb, hw);
+                for (int o = hw >> 1; o > 0; o >>= 1) {
+                    v += __shfl_xor_sync(0xffffffffu, v, o);
+                }
+                if ((l & (hw - 1)) == 0 && (up ? v1 : v0)) {
+                    pout[B.prof_off + X0 + (up ? 1 : 0)] = v;
+                }
+            }
+        }
+        mc = mn;
+        lo_c = lo_n;
+        hi_c = hi_n;
     }
     if (bad && threadIdx.x == 0) {
         atomicCAS(status, 0, VFPS_ERR_TIMEOUT);

@@ -170,6 +170,37 @@ def test_batch_tilings_agree(gpu_ctx, monkeypatch):
         assert rel_l1(got, ref.density(0)) <= TOL, i
 
 
+def test_batch_wide_meshes(gpu_ctx):
+    """Meshes of 512 and 1024 rows (the wide chain-0 kernel) next to
+    narrow ones (the ring kernel) in one batch, against the FP64 oracle."""
+    specs, z_by_n, zdata = [], {}, {}
+    for n in (128, 512, 1024):
+        spt = 1000 if n < 1024 else 2000
+        p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                      VacuumGap=0.0318)
+        z_by_n[n] = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p0))
+        zdata[n] = z_by_n[n].data()
+    for n, S, it in ((512, 0.4, 4), (128, 0.9, 3), (1024, 1.2, 4),
+                     (512, 1.4, 2)):
+        spt = 1000 if n < 1024 else 2000
+        p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                     VacuumGap=0.0318, S_csr=S)
+        specs.append((p, 0, p["Ib"], it, False))
+    b = make_batch(gpu_ctx, specs, z_by_n)
+    steps = 24
+    b.step(steps)
+    assert gpu_ctx.device_status() == 0
+    dens = b.download()
+    for i, (p, ch, ib, it, cl) in enumerate(specs):
+        n = p["ps_bins"]
+        ref = oracle_sim(p, ch, ib, zdata[n], it=it, clamp=cl)
+        ref.step(steps)
+        off, _ = b.layout(i)
+        got = dens[off:off + n * n].reshape(n, n)
+        assert rel_l1(got, ref.density(0)) <= TOL, (i, n)
+        assert rel_l1(b.profile(i), ref.profile(0)) <= TOL, (i, n)
+
+
 def test_batch_equals_plain_loop(gpu_ctx):
     """The fused kernel and the one-map-per-launch loop agree."""
     n = 128
