@@ -25,6 +25,7 @@
 #include <cstdlib>
 #include <map>
 #include <mutex>
+#include <string>
 
 #include "vfps_internal.cuh"
 
@@ -54,6 +55,7 @@ struct vfps_batch {
     DevBuf<uint32_t> row_bunch;
     DevBuf<float> dens[2], prof[2];
     DevBuf<float> wake, factor;
+    DevBuf<RowInfo> rinfo;     // chain-0 y-kick stencils of every row
     DevBuf<double> filling;
     DevBuf<unsigned> counters;
     int cur = 0;               // buffer holding the current state
@@ -150,24 +152,24 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
                         + std::max<size_t>(1024, b->max_n)) * sizeof(float);
     mark(0);
     k_bwake<<<b->nb, THREADS, wsm, st>>>(
-        b->bd.p, b->tabs.p, b->wt.p, b->prof[from].p, b->wake.p, b->factor.p,
-        b->filling.p, b->counters.p, b->ctx->d_status);
+        b->bd.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p, b->wake.p,
+        b->rinfo.p, b->factor.p, b->filling.p, b->counters.p,
+        b->ctx->d_status);
     VFPS_LAUNCHED();
     mark(1);
     if (!b->htiles[TL_RING].empty()) {
         k_bmaps0<<<b->gridR, RTHREADS, b->smem[TL_RING], st>>>(
             b->bd.p, b->tiles[TL_RING].p,
             static_cast<uint32_t>(b->htiles[TL_RING].size()), b->tabs.p,
-            b->st.p, b->fp5.p, b->dwt.p, b->wake.p, b->factor.p,
-            b->dens[from].p, b->dens[to].p, b->prof[to].p, b->ctx->d_status,
-            b->layoutR);
+            b->dwt.p, b->rinfo.p, b->dens[from].p, b->dens[to].p,
+            b->prof[to].p, b->ctx->d_status, b->layoutR);
         VFPS_LAUNCHED();
     }
     if (!b->htiles[TL_WIDE].empty()) {
         k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], st>>>(
             b->bd.p, b->tiles[TL_WIDE].p,
             static_cast<uint32_t>(b->htiles[TL_WIDE].size()), b->tabs.p,
-            b->st.p, b->fp5.p, b->wake.p, b->factor.p, b->dens[from].p,
+            b->st.p, b->fp5.p, b->rinfo.p, b->dens[from].p,
             b->dens[to].p, b->prof[to].p, b->ctx->d_status, b->layout0);
         VFPS_LAUNCHED();
     }
@@ -598,6 +600,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         b->desc.assign(desc, desc + nb);
         b->hb.resize(nb);
         std::vector<float> tabs, fp5, wt, gauss, dwt;
+        std::map<std::string, uint32_t> dw_seen;
         std::vector<RowStencil> sts;
         std::vector<uint32_t> row_bunch, goff;
         std::vector<uint32_t> wt_off(nimp, 0xffffffffu);
@@ -713,17 +716,45 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             sts.insert(sts.end(), dr.begin(), dr.end());
             if (d.chain == 0) {
                 // drift stencils as planes for 16-byte loads: w[j][y] for
-                // j < 4, then shift0[y] (int bits)
-                B.dw_off = static_cast<uint32_t>(dwt.size());
+                // j < 4, then shift0[y] (int bits), then the Fokker-Planck
+                // weights as planes F[o][y] for the offsets -2..2 (the
+                // identity without Fokker-Planck)
+                std::vector<float> tab;
+                tab.reserve(size_t(n) * 10);
                 for (int j = 0; j < 4; j++) {
                     for (uint32_t y = 0; y < n; y++) {
-                        dwt.push_back(dr[y].w[j]);
+                        tab.push_back(dr[y].w[j]);
                     }
                 }
                 for (uint32_t y = 0; y < n; y++) {
                     float f;
                     std::memcpy(&f, &dr[y].shift0, sizeof(f));
-                    dwt.push_back(f);
+                    tab.push_back(f);
+                }
+                std::vector<float> w5(size_t(n) * 5, 0.f);
+                if (d.e1 > 0) {
+                    w5 = fp_weights(ay, float(d.e1), d.fptype, d.derivation);
+                } else {
+                    for (uint32_t y = 0; y < n; y++) {
+                        w5[size_t(y) * 5 + 2] = 1.f;
+                    }
+                }
+                for (int o = 0; o < 5; o++) {
+                    for (uint32_t y = 0; y < n; y++) {
+                        tab.push_back(w5[size_t(y) * 5 + o]);
+                    }
+                }
+                // bunches of a scan share these tables: one copy each, so
+                // that they stay in L1
+                std::string key(reinterpret_cast<const char*>(tab.data()),
+                                tab.size() * sizeof(float));
+                auto it = dw_seen.find(key);
+                if (it != dw_seen.end()) {
+                    B.dw_off = it->second;
+                } else {
+                    B.dw_off = static_cast<uint32_t>(dwt.size());
+                    dw_seen.emplace(std::move(key), B.dw_off);
+                    dwt.insert(dwt.end(), tab.begin(), tab.end());
                 }
             }
             if (d.e1 > 0) {
@@ -804,6 +835,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             VFPS_CUDA(cudaMemsetAsync(b->prof[k].p, 0, b->prof[k].bytes(), st));
         }
         b->wake.alloc(b->rows);
+        b->rinfo.alloc(b->rows);
+        VFPS_CUDA(cudaMemsetAsync(b->rinfo.p, 0, b->rinfo.bytes(), st));
         VFPS_CUDA(cudaMemsetAsync(b->wake.p, 0, b->wake.bytes(), st));
         b->factor.alloc(nb);
         b->filling.alloc(nb);

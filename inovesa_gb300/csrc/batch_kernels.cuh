@@ -52,13 +52,14 @@ struct RowStencil {
     float w[4];
 };
 
-// per staged row of chain 0: combined shift of the two y-kicks and their
-// weights
-struct RowInfo {
+// per mesh row of chain 0: combined shift of the two y-kicks and their
+// weights (built by k_bwake once per step; 48 bytes, three 16-byte loads)
+struct __align__(16) RowInfo {
     int s;      // sa + sb
     int sb;     // shift of the second (RF) kick
     float a[4]; // wake kick weights (times the renormalisation factor)
     float b[4]; // RF kick weights
+    int pad[2];
 };
 
 enum { F_WAKE = 1, F_FP = 2, F_CLAMP = 4 };
@@ -109,14 +110,16 @@ __device__ __forceinline__ RowStencil make_stencil(float offset, uint32_t n,
 // ----------------------------------------------------------------- wake
 __global__ void __launch_bounds__(THREADS)
 k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
-        const float* __restrict__ wt, const float* __restrict__ pin,
-        float* __restrict__ wake, float* __restrict__ factor,
+        const float* __restrict__ wt, const RowStencil* __restrict__ st,
+        const float* __restrict__ pin, float* __restrict__ wake,
+        RowInfo* __restrict__ rinfo, float* __restrict__ factor,
         double* __restrict__ filling, unsigned* __restrict__ counters,
         int* __restrict__ status)
 {
     extern __shared__ float4 wsm4[];
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
     __shared__ double red[32];
+    __shared__ float fac_s;
     const uint32_t b = blockIdx.x;
     const BDev B = bd[b];
     const int n = int(B.n);
@@ -181,6 +184,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             v = __fmul_rn(B.wakescale, s);
         }
         wake[B.prof_off + x] = v;
+        partial[x] = v;    // this thread read partial[.][x] last
     }
     // charge integral (src/PS/PhaseSpace.cpp:200-239) in FP64
     const float* ws = tabs + B.tab_off + TAB_WS * n;
@@ -198,6 +202,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             f = B.fillset > 0 ? static_cast<float>(double(B.fillset) / a) : 0.f;
         }
         factor[b] = f;
+        fac_s = f;
         if (B.fillset > 0 && !(a > 0)) {
             atomicCAS(status, 0, VFPS_ERR_NUMERIC);
         }
@@ -209,6 +214,35 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             counters[0] = step + 1;
             __threadfence();
         }
+    }
+    if (B.chain != 0) {
+        return;
+    }
+    // chain 0: both y-kick stencils of every row for this step, the
+    // renormalisation factor folded into the first (both kicks are linear)
+    __syncthreads();
+    const float fac = fac_s;
+    const RowStencil* rf = st + B.st_off + ST_RF * n;
+    for (int x = threadIdx.x; x < n; x += THREADS) {
+        RowStencil sa;
+        if (has_wake) {
+            sa = make_stencil(partial[x], B.n, int(B.it));
+        } else {
+            sa.shift0 = 0;
+            sa.w[0] = 1.f;
+            sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
+        }
+        const RowStencil sb = rf[x];
+        RowInfo ri;
+        ri.s = sa.shift0 + sb.shift0;
+        ri.sb = sb.shift0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            ri.a[j] = sa.w[j] * fac;
+            ri.b[j] = sb.w[j];
+        }
+        ri.pad[0] = ri.pad[1] = 0;
+        rinfo[B.prof_off + x] = ri;
     }
 }
 
@@ -401,7 +435,7 @@ __global__ void __launch_bounds__(THREADS, 2)
 k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          uint32_t ntiles, const float* __restrict__ tabs,
          const RowStencil* __restrict__ st, const float* __restrict__ fp5,
-         const float* __restrict__ wake, const float* __restrict__ factor,
+         const RowInfo* __restrict__ rinfo,
          const float* __restrict__ din, float* __restrict__ dout,
          float* __restrict__ pout, int* __restrict__ status, Smem0 L)
 {
@@ -458,7 +492,6 @@ k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         const int hlo = B.halo_lo, hhi = B.halo_hi;
         const int nr = rows + hlo + hhi;
         const int as = astride0(n);
-        const int it = int(B.it);
         float* A = cur ? A1 : A0;
         if (t.bunch != cached) {
             cached = t.bunch;
@@ -480,32 +513,13 @@ k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             }
         }
 
-        // per staged row: wake kick (this step) and RF kick (static)
+        // per staged row: both y-kick stencils of this step
         {
-            const float fac = factor[t.bunch];
-            const RowStencil* rf = st + B.st_off + ST_RF * n;
             for (int r = threadIdx.x; r < nr; r += THREADS) {
                 const int x = x0 - hlo + r;
                 RowInfo ri;
                 if (unsigned(x) < unsigned(n)) {
-                    RowStencil sa;
-                    if (B.flags & F_WAKE) {
-                        sa = make_stencil(wake[B.prof_off + x], B.n, it);
-                    } else {
-                        sa.shift0 = 0;
-                        sa.w[0] = 1.f;
-                        sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
-                    }
-                    const RowStencil sb = rf[x];
-                    ri.s = sa.shift0 + sb.shift0;
-                    ri.sb = sb.shift0;
-#pragma unroll
-                    for (int j = 0; j < 4; j++) {
-                        // the renormalisation factor rides on the first
-                        // kick (both kicks are linear)
-                        ri.a[j] = sa.w[j] * fac;
-                        ri.b[j] = sb.w[j];
-                    }
+                    ri = rinfo[B.prof_off + x];
                 } else {
                     ri.s = 0;
                     ri.sb = 0;
@@ -660,74 +674,12 @@ constexpr int RTHREADS = 128;
 
 struct SmemR {
     uint32_t ring;  // RB slots of RS floats
-    uint32_t s;     // RowInfo of the rows staged for one tile
+    uint32_t s;     // RowInfo of the new rows of one tile
     uint32_t bar;   // two mbarriers
     uint32_t rb;    // ring slots (power of two)
     uint32_t rs;    // floats per slot
     uint32_t total;
 };
-
-// Fokker-Planck weights (offsets -2..2) of the 8 columns a lane owns,
-// [group * 4 + column], and the Simpson step h03 = delta/3 (the weights are
-// h03 at both ends of the row, else 4 h03 at odd and 2 h03 at even columns)
-struct FpCols2 {
-    float f[8][5];
-    float h03;
-};
-
-__device__ __forceinline__ int lane_col(int n, int l, int k)
-{
-    return (k >> 2) * (n >> 1) + 4 * l + (k & 3);
-}
-
-__device__ __forceinline__ void load_fp_cols2(const BDev& B,
-                                              const float* __restrict__ fp5,
-                                              const float* __restrict__ ws,
-                                              FpCols2& c)
-{
-    const int n = int(B.n);
-    const int l = threadIdx.x % (n >> 3);
-    const bool has_fp = B.flags & F_FP;
-    c.h03 = ws[0];
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        const int y = lane_col(n, l, k);
-#pragma unroll
-        for (int o = 0; o < 5; o++) {
-            c.f[k][o] = has_fp ? fp5[B.fp_off + y * 5 + o]
-                               : (o == 2 ? 1.f : 0.f);
-        }
-    }
-}
-
-// wake (times the renormalisation factor) and RF y-kick stencils of mesh
-// row x
-__device__ __forceinline__ RowInfo row_info(const BDev& B, int x,
-                                            const float* __restrict__ wake,
-                                            const RowStencil* __restrict__ rf,
-                                            float fac)
-{
-    RowStencil sa;
-    if (B.flags & F_WAKE) {
-        sa = make_stencil(wake[B.prof_off + x], B.n, int(B.it));
-    } else {
-        sa.shift0 = 0;
-        sa.w[0] = 1.f;
-        sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
-    }
-    const RowStencil sb = rf[x];
-    RowInfo ri;
-    ri.s = sa.shift0 + sb.shift0;
-    ri.sb = sb.shift0;
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        // the renormalisation factor rides on the first kick (both kicks
-        // are linear)
-        ri.a[j] = sa.w[j] * fac;
-        ri.b[j] = sb.w[j];
-    }
-    return ri;
-}
 
 // t2[i] = sum_j a_j c[AL + i + j] for the 7 positions the second kick of
 // 4 cells reads
@@ -811,21 +763,25 @@ struct RingMap {
     }
 };
 
-// bulk copies of the mesh rows among [lo, hi) into their slots (warp 0;
-// lane 0 arms the barrier with the byte count first)
+// bulk copies of the mesh rows among [lo, hi) into their slots, and of
+// their y-kick stencils into S[x - lo] (warp 0; lane 0 arms the barrier
+// with the byte count first)
 __device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
                                            const RingMap& m, float* ring,
                                            int rb, int rs,
                                            const float* __restrict__ din,
-                                           uint64_t* bar)
+                                           const RowInfo* __restrict__ rinfo,
+                                           RowInfo* S, uint64_t* bar)
 {
     const int n = int(B.n);
     const int a = max(lo, 0), e = min(hi, n);
     const uint32_t row_bytes = uint32_t(n) * 4u;
+    const uint32_t ri_bytes = uint32_t(e - a) * uint32_t(sizeof(RowInfo));
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         fence_proxy_async();
-        mbar_arrive_expect_tx(bar, uint32_t(e - a) * row_bytes);
+        mbar_arrive_expect_tx(bar, uint32_t(e - a) * row_bytes + ri_bytes);
+        tma_load_1d(S + (a - lo), rinfo + B.prof_off + a, ri_bytes, bar);
     }
     __syncwarp();
     for (int x = a + lane; x < e; x += 32) {
@@ -899,72 +855,103 @@ __device__ __forceinline__ void drift2(const float* ring, const RingMap& m,
     }
 }
 
-// Fokker-Planck of one row's 8 lane cells from their drift values d[8]
-// (group A then group B) and the neighbours' (shuffles within the row's
-// seg lanes); stores the row and returns its projection partial
-__device__ __forceinline__ float fp_row(const float* d, int l, int seg,
-                                        const FpCols2& cc, float* dst_a,
-                                        float* dst_b, bool valid)
+// Fokker-Planck of two rows (d0, d1: their 8 lane cells after the drift,
+// group A then group B) with the neighbours' cells taken by shuffles
+// within the row's seg lanes; the weights of a group's 4 columns come as
+// 5 planes F[o][y] (offsets -2..2).  Stores the rows (where valid) and
+// returns their Simpson-weighted partial sums (in units of h03: the
+// weights alternate 2, 4 along the row, 1 at both ends).
+__device__ __forceinline__ void fp_rows2(const float* d0, const float* d1,
+                                         int l, int seg, int n,
+                                         const float* __restrict__ F,
+                                         float* o0, float* o1, bool v0,
+                                         bool v1, float& p0, float& p1)
 {
     const int lp = (l + 1) & (seg - 1), lm = (l + seg - 1) & (seg - 1);
-    const float rA0 = __shfl_sync(0xffffffffu, d[0], lp, seg);
-    const float rA1 = __shfl_sync(0xffffffffu, d[1], lp, seg);
-    const float rB0 = __shfl_sync(0xffffffffu, d[4], lp, seg);
-    const float rB1 = __shfl_sync(0xffffffffu, d[5], lp, seg);
-    const float lA2 = __shfl_sync(0xffffffffu, d[2], lm, seg);
-    const float lA3 = __shfl_sync(0xffffffffu, d[3], lm, seg);
-    const float lB2 = __shfl_sync(0xffffffffu, d[6], lm, seg);
-    const float lB3 = __shfl_sync(0xffffffffu, d[7], lm, seg);
     const bool first = l == 0, last = l == seg - 1;
-    // columns -2..5 around each group
-    const float wa[8] = {first ? 0.f : lA2, first ? 0.f : lA3, d[0], d[1],
-                         d[2], d[3], last ? rB0 : rA0, last ? rB1 : rA1};
-    const float wb[8] = {first ? lA2 : lB2, first ? lA3 : lB3, d[4], d[5],
-                         d[6], d[7], last ? 0.f : rB0, last ? 0.f : rB1};
-    float out[8];
+    // columns 2, 3 of the left lane's group A (group A's left neighbours,
+    // and group B's on lane 0) and columns 0, 1 of the right lane's group B
+    // (group B's right neighbours, and group A's on the last lane)
+    float la[2][2], rb_[2][2];
 #pragma unroll
-    for (int c = 0; c < 4; c++) {
-        float v = cc.f[c][0] * wa[c];
-        v = fmaf(cc.f[c][1], wa[c + 1], v);
-        v = fmaf(cc.f[c][2], wa[c + 2], v);
-        v = fmaf(cc.f[c][3], wa[c + 3], v);
-        v = fmaf(cc.f[c][4], wa[c + 4], v);
-        out[c] = v;
-        float u = cc.f[4 + c][0] * wb[c];
-        u = fmaf(cc.f[4 + c][1], wb[c + 1], u);
-        u = fmaf(cc.f[4 + c][2], wb[c + 2], u);
-        u = fmaf(cc.f[4 + c][3], wb[c + 3], u);
-        u = fmaf(cc.f[4 + c][4], wb[c + 4], u);
-        out[4 + c] = u;
+    for (int r = 0; r < 2; r++) {
+        const float* d = r ? d1 : d0;
+        la[r][0] = __shfl_sync(0xffffffffu, d[2], lm, seg);
+        la[r][1] = __shfl_sync(0xffffffffu, d[3], lm, seg);
+        rb_[r][0] = __shfl_sync(0xffffffffu, d[4], lp, seg);
+        rb_[r][1] = __shfl_sync(0xffffffffu, d[5], lp, seg);
     }
-    if (valid) {
-        *reinterpret_cast<float4*>(dst_a) =
-            make_float4(out[0], out[1], out[2], out[3]);
-        *reinterpret_cast<float4*>(dst_b) =
-            make_float4(out[4], out[5], out[6], out[7]);
+    float pe[2] = {0.f, 0.f}, po[2] = {0.f, 0.f};
+#pragma unroll
+    for (int g = 0; g < 2; g++) {
+        const int y = g * (n >> 1) + 4 * l;
+        float f[5][4];
+#pragma unroll
+        for (int o = 0; o < 5; o++) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(
+                F + o * n + y));
+            f[o][0] = v.x; f[o][1] = v.y; f[o][2] = v.z; f[o][3] = v.w;
+        }
+#pragma unroll
+        for (int r = 0; r < 2; r++) {
+            const float* d = (r ? d1 : d0) + 4 * g;
+            float w[8];
+            if (g == 0) {
+                const float rA0 = __shfl_sync(0xffffffffu, d[0], lp, seg);
+                const float rA1 = __shfl_sync(0xffffffffu, d[1], lp, seg);
+                w[0] = first ? 0.f : la[r][0];
+                w[1] = first ? 0.f : la[r][1];
+                w[6] = last ? rb_[r][0] : rA0;
+                w[7] = last ? rb_[r][1] : rA1;
+            } else {
+                const float lB2 = __shfl_sync(0xffffffffu, d[2], lm, seg);
+                const float lB3 = __shfl_sync(0xffffffffu, d[3], lm, seg);
+                w[0] = first ? la[r][0] : lB2;
+                w[1] = first ? la[r][1] : lB3;
+                w[6] = last ? 0.f : rb_[r][0];
+                w[7] = last ? 0.f : rb_[r][1];
+            }
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                w[2 + c] = d[c];
+            }
+            float out[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                float v = f[0][c] * w[c];
+                v = fmaf(f[1][c], w[c + 1], v);
+                v = fmaf(f[2][c], w[c + 2], v);
+                v = fmaf(f[3][c], w[c + 3], v);
+                v = fmaf(f[4][c], w[c + 4], v);
+                out[c] = v;
+            }
+            if (r ? v1 : v0) {
+                *reinterpret_cast<float4*>((r ? o1 : o0) + y) =
+                    make_float4(out[0], out[1], out[2], out[3]);
+            }
+            // Simpson weights along the row: even columns 2, odd 4, with
+            // column 0 (lane 0, group A) and n - 1 (last lane, group B) 1
+            float e = out[0] + out[2], od = out[1] + out[3];
+            if (g == 0 && first) {
+                e -= 0.5f * out[0];
+            }
+            if (g == 1 && last) {
+                od -= 0.75f * out[3];
+            }
+            pe[r] += e;
+            po[r] += od;
+        }
     }
-    // Simpson-weighted partial sum: lane columns alternate even, odd, so
-    // the weights are 2 h03, 4 h03 except for columns 0 and n - 1 (h03)
-    const float pe = (out[0] + out[2]) + (out[4] + out[6]);
-    const float po = (out[1] + out[3]) + (out[5] + out[7]);
-    float pp = fmaf(4.f, po, 2.f * pe);
-    if (first) {
-        pp -= out[0];
-    }
-    if (last) {
-        pp = fmaf(-3.f, out[7], pp);
-    }
-    return cc.h03 * pp;
+    p0 = fmaf(4.f, po[0], 2.f * pe[0]);
+    p1 = fmaf(4.f, po[1], 2.f * pe[1]);
 }
 
 __global__ void __launch_bounds__(RTHREADS, 4)
 k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          uint32_t ntiles, const float* __restrict__ tabs,
-         const RowStencil* __restrict__ st, const float* __restrict__ fp5,
-         const float* __restrict__ dwt, const float* __restrict__ wake,
-         const float* __restrict__ factor, const float* __restrict__ din,
-         float* __restrict__ dout, float* __restrict__ pout,
-         int* __restrict__ status, SmemR L)
+         const float* __restrict__ dwt, const RowInfo* __restrict__ rinfo,
+         const float* __restrict__ din, float* __restrict__ dout,
+         float* __restrict__ pout, int* __restrict__ status, SmemR L)
 {
     extern __shared__ float4 smem4[];
     char* base = reinterpret_cast<char*>(smem4);
@@ -1009,12 +996,11 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         mc = RingMap{lo_c, 0};
         front = hi_c - lo_c;
         if (warp == 0) {
-            issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, &bar[0]);
+            issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, rinfo, S,
+                       &bar[0]);
         }
     }
     int bad = 0;
-    uint32_t cached = 0xffffffffu;
-    FpCols2 fpc;
     for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
         const Tile t = tiles[tid];
         const BDev B = bd[t.bunch];
@@ -1026,29 +1012,10 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         const int rl = threadIdx.x / seg;
         const int rp = RTHREADS / seg;
         const int as = astride0(n);
-        if (t.bunch != cached) {
-            cached = t.bunch;
-            load_fp_cols2(B, fp5, tabs + B.tab_off + TAB_WS * n, fpc);
-        }
 
-        // stage 1: RowInfo of the new rows this warp owns (lane q of the
-        // warp takes the q-th of them), then their y-kicks in place
+        // stage 1: both y-kicks of the new rows, in place
         {
             const int m = hi_c - lo_c;
-            const int rpw = 32 / seg;          // rows side by side in a warp
-            const float fac = factor[t.bunch];
-            const RowStencil* rf = st + B.st_off + ST_RF * n;
-            for (int q = lane; ; q += 32) {
-                const int i = warp * rpw + q % rpw + (q / rpw) * rp;
-                if (i >= m) {
-                    break;
-                }
-                const int x = lo_c + i;
-                if (unsigned(x) < unsigned(n)) {
-                    S[i] = row_info(B, x, wake, rf, fac);
-                }
-            }
-            __syncwarp();
             if (!mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, WAIT_NS)) {
                 bad = 1;
                 mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, WAIT_NS);
@@ -1066,8 +1033,8 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                     reinterpret_cast<float4*>(row + APAD + n)[j] = z;
                 }
                 if (unsigned(x) < unsigned(n)) {
-                    __syncwarp(rmask);
                     const RowInfo ri = S[i];
+                    __syncwarp(rmask);
                     const int ya = 4 * l, yb = (n >> 1) + 4 * l;
                     const float4 oa = ykick4(row, as, n, ya, ri);
                     const float4 ob = ykick4(row, as, n, yb, ri);
@@ -1101,7 +1068,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             }
             front = hi_n - mn.xref + mn.pref;
             if (warp == 0) {
-                issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din,
+                issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo, S,
                            &bar[(k + 1) & 1]);
             }
         }
@@ -1109,7 +1076,9 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         // drift x-kick, Fokker-Planck, output rows and projections, two
         // rows per lane segment
         {
-            const float* W = dwt + B.dw_off;
+            const float* W = dwt + B.dw_off;      // drift planes [5][n]
+            const float* F = W + 5 * n;           // Fokker-Planck [5][n]
+            const float h03 = tabs[B.tab_off + TAB_WS * n];
             const int hw = seg >> 1;
             for (int rbase = 0; rbase < rows; rbase += 2 * rp) {
                 const int r0 = rbase + 2 * rl;
@@ -1120,10 +1089,8 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 drift2(ring, mc, rb, rs, X0, (n >> 1) + 4 * l, W, n, d0 + 4,
                        d1 + 4);
                 float* o0 = dout + B.dens_off + size_t(X0) * n;
-                const float pa = fp_row(d0, l, seg, fpc, o0 + 4 * l,
-                                        o0 + (n >> 1) + 4 * l, v0);
-                const float pb = fp_row(d1, l, seg, fpc, o0 + n + 4 * l,
-                                        o0 + n + (n >> 1) + 4 * l, v1);
+                float pa, pb;
+                fp_rows2(d0, d1, l, seg, n, F, o0, o0 + n, v0, v1, pa, pb);
                 // row sums of both rows in one butterfly: the lower half of
                 // the segment sums row r0, the upper half row r0 + 1
                 const bool up = (l & hw) != 0;
@@ -1133,7 +1100,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                     v += __shfl_xor_sync(0xffffffffu, v, o);
                 }
                 if ((l & (hw - 1)) == 0 && (up ? v1 : v0)) {
-                    pout[B.prof_off + X0 + (up ? 1 : 0)] = v;
+                    pout[B.prof_off + X0 + (up ? 1 : 0)] = h03 * v;
                 }
             }
         }
