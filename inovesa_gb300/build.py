@@ -81,6 +81,30 @@ def build(force=False, verbose=False, extra_flags=()):
     return LIB
 
 
+DRIVER = os.path.join(OUT, "vfps_solver")
+
+
+def build_driver(force=False):
+    """The C++ solver driver over include/vfps.hpp, linked to libvfps.so
+    (found next to it at run time)."""
+    lib = build()
+    src = os.path.join(HERE, "cpp", "vfps_solver.cpp")
+    deps = [src, lib, os.path.join(ROOT, "include", "vfps.hpp"),
+            os.path.join(ROOT, "include", "vfps.h")]
+    if not force and not _stale(DRIVER, deps):
+        return DRIVER
+    cxx = shutil.which("g++") or "g++"
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-Wextra", "-I",
+           os.path.join(ROOT, "include"), src, "-L", OUT, "-lvfps",
+           "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s%s" % (r.stdout, r.stderr))
+    os.replace(tmp, DRIVER)
+    return DRIVER
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv,
                 extra_flags=[a for a in sys.argv[1:] if a.startswith("-X")]))

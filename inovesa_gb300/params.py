@@ -175,3 +175,32 @@ def csr_impedance_args(p):
     """makeImpedance for the radiated CSR (src/main.cpp:723-727)."""
     return dict(nfreqs=p["padded_bins"], fmax=p["fmax"], R_bend=p["R_bend"],
                 frev=p["f_rev"], gap=p["gap"] if p["gap"] > 0 else -1.0)
+
+
+def run_file(p, chain=0, it=None, clamp=False, steps=1, csr=False, Ib=None):
+    """The "key = value" run file of the C++ solver driver
+    (inovesa_gb300/cpp/vfps_solver.cpp) for derived parameters p."""
+    o = p["opts"]
+    a = p["axes"]
+    w = wake_impedance_args(p)
+    c = csr_impedance_args(p)
+    slip = [float(v) for v in p["slip"]]
+    kv = dict(
+        n=p["ps_bins"], chain=chain,
+        it=int(o["InterpolationPoints"] if it is None else it),
+        clamp=int(bool(clamp)), renormalize=int(o["RenormalizeCharge"]),
+        qmin=a[0], qmax=a[1], qscale=a[2], pmin=a[3], pmax=a[4], pscale=a[5],
+        Ib=p["Ib"] if Ib is None else Ib, f_rev=p["f_rev"],
+        zoom=o["InitialDistZoom"], padded_bins=w["nfreqs"], fmax=w["fmax"],
+        R_bend=w["R_bend"], gap=w["gap"], use_csr=int(w["use_csr"]),
+        s=w["s"], xi=w["xi"], coll=w["inner_coll_radius"],
+        csr_gap=c["gap"], spacing_bins=p["spacing_bins"],
+        revolutionpart=p["revolutionpart"], E0=p["E0"], sE=p["sE"],
+        dt=p["dt"], linear_rf=int(bool(o["LinearRF"])), angle=p["angle"],
+        f_RF=p["f_RF"], V_eff=p["V_eff"], V0=p["V0"], nslip=len(slip),
+        e1=p["e1"], fptype=int(o["FPType"]), fptrack=int(o["FPTrack"]),
+        derivation=int(o["derivation"]), fc=p["fc"], csr=int(bool(csr)),
+        steps=int(steps))
+    for k, v in enumerate(slip):
+        kv["slip%d" % k] = v
+    return "".join("%s = %r\n" % (k, float(v)) for k, v in kv.items())
