@@ -257,6 +257,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--wake-mode", type=int, default=0, choices=[0, 1],
+                    help="wake potentials on the CUDA cores (0) or the "
+                         "tensor cores (1); the other mode is measured "
+                         "alongside")
     ap.add_argument("--profile", action="store_true",
                     help="timed steps only (for ncu): no e2e, plain loop or "
                          "CPU legs")
@@ -289,6 +293,7 @@ def main():
     ctx = V.Context(local)
     z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
     batch = make_batch(ctx, p, currents, z)
+    batch.set_wake_mode(args.wake_mode)
     cells = batch.cells
     stream = torch.cuda.ExternalStream(
         _lib.lib().vfps_stream(ctx.handle), device=local)
@@ -358,6 +363,28 @@ def main():
         for k, v in batch.kernel_times(1).items():
             kt[k] = kt.get(k, 0.0) + v / nk
 
+    # the other wake mode: kernel times and back-to-back steps
+    other = 1 - args.wake_mode
+    batch.set_wake_mode(other)
+    batch.step(8)
+    kt_o = {}
+    for _ in range(nk):
+        flush_l2()
+        for k, v in batch.kernel_times(1).items():
+            kt_o[k] = kt_o.get(k, 0.0) + v / nk
+    o0 = torch.cuda.Event(enable_timing=True)
+    o1 = torch.cuda.Event(enable_timing=True)
+    o0.record(stream)
+    batch.step(args.steps)
+    o1.record(stream)
+    o1.synchronize()
+    other_cont = cells * args.steps / (o0.elapsed_time(o1) / 1e3)
+    batch.set_wake_mode(args.wake_mode)
+    if ctx.device_status() != 0:
+        print(json.dumps({"error": "device status after the wake-mode run"}),
+              flush=True)
+        sys.exit(3)
+
     # end to end through the C ABI with pinned host buffers: each call is
     # one output interval of the reference (100 solver steps): density in,
     # steps, density, profiles and fillings out
@@ -421,6 +448,10 @@ def main():
                      "kernel_ms": ms_maps},
         "kernel_ms_per_step": kt,
         "continuous_value": continuous,
+        "wake_mode": ["cuda cores", "tensor cores"][args.wake_mode],
+        "other_wake_mode": {
+            "wake_mode": ["cuda cores", "tensor cores"][other],
+            "kernel_ms_per_step": kt_o, "continuous_value": other_cont},
         "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes + batch.rows * 4 + NB * 4,

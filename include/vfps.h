@@ -347,6 +347,13 @@ VFPS_API int vfps_batch_info(const vfps_batch* batch, uint32_t* launches,
 VFPS_API int vfps_batch_kernel_times(vfps_batch* batch, uint32_t nsteps,
                                      float* ms);
 
+/* Where the batch computes the wake potentials (no counterpart in the
+ * reference): mode 0 (default) on the CUDA cores inside the per-bunch wake
+ * kernel; mode 1 as one Toeplitz x profiles product per group of bunches
+ * sharing an impedance and mesh size, on the tensor cores (TF32 split into
+ * three products, FP32 accumulation: FP32-level accuracy). */
+VFPS_API int vfps_batch_set_wake_mode(vfps_batch* batch, int mode);
+
 /* ------------------------------------------------- no-allocation helper
  * No counterpart in the reference.  Charge integral of nb meshes [n][n]
  * that the caller already holds in device memory (density = device

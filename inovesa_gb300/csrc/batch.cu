@@ -30,6 +30,7 @@
 #include "vfps_internal.cuh"
 
 #include "batch_kernels.cuh"
+#include "wake_tc.cuh"
 
 using vfps::DevBuf;
 
@@ -66,6 +67,13 @@ struct vfps_batch {
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
+    // wake potentials on the tensor cores (k_wake_tc) instead of inside
+    // k_bwake: Toeplitz planes per (impedance, mesh size) and bunch tiles
+    int wake_tc = 0;
+    DevBuf<float> tplanes;
+    DevBuf<TcGroup> tcg;
+    DevBuf<uint32_t> tclist;
+    uint32_t tc_groups = 0;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 1 step from buffer i
     cudaGraphExec_t graph8[2] = {nullptr, nullptr}; // 8 steps from buffer i
 };
@@ -151,10 +159,18 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     const size_t wsm = (3 * size_t(b->max_n)
                         + std::max<size_t>(1024, b->max_n)) * sizeof(float);
     mark(0);
+    const bool tc = b->wake_tc && b->tc_groups > 0;
+    if (tc) {
+        const dim3 grid((b->max_n + TC_M - 1) / TC_M, b->tc_groups);
+        k_wake_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(
+            b->bd.p, b->tcg.p, b->tclist.p, b->tplanes.p, b->prof[from].p,
+            b->wake.p, b->ctx->d_status);
+        VFPS_LAUNCHED();
+    }
     k_bwake<<<b->nb, THREADS, wsm, st>>>(
         b->bd.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p, b->wake.p,
         b->rinfo.p, b->factor.p, b->filling.p, b->counters.p,
-        b->ctx->d_status);
+        b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
     if (!b->htiles[TL_RING].empty()) {
@@ -827,6 +843,69 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                                             b->wt.p + wt_off[k]);
             }
         }
+        // Toeplitz planes T[x][m] = w[(x - m) mod nmax] of every (impedance,
+        // mesh size) pair (hi and lo parts for the tensor cores) and the
+        // bunch tiles that share them
+        {
+            std::vector<float> wt_host(wt.size());
+            VFPS_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (!wt.empty()) {
+                VFPS_CUDA(cudaMemcpy(wt_host.data(), b->wt.p,
+                                     wt.size() * sizeof(float),
+                                     cudaMemcpyDeviceToHost));
+            }
+            std::vector<float> tp;
+            std::vector<TcGroup> groups;
+            std::vector<uint32_t> tl;
+            std::map<std::pair<uint32_t, uint32_t>, uint32_t> t_at;
+            std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>>
+                members;
+            for (uint32_t i = 0; i < nb; i++) {
+                const BDev& B = b->hb[i];
+                if (!(B.flags & F_WAKE)) {
+                    continue;
+                }
+                const auto key = std::make_pair(B.wt_off, B.n);
+                members[key].push_back(i);
+                if (t_at.count(key)) {
+                    continue;
+                }
+                t_at[key] = static_cast<uint32_t>(tp.size());
+                const uint32_t nn = B.n, nmax = B.nmax;
+                const float* w = wt_host.data() + B.wt_off;
+                const size_t hi0 = tp.size();
+                tp.resize(hi0 + 2 * size_t(nn) * nn);
+                for (uint32_t x = 0; x < nn; x++) {
+                    for (uint32_t m = 0; m < nn; m++) {
+                        const float v = w[(x + nmax - m) % nmax];
+                        const float h = tf32_hi(v);
+                        tp[hi0 + size_t(x) * nn + m] = h;
+                        tp[hi0 + size_t(nn) * nn + size_t(x) * nn + m] = v - h;
+                    }
+                }
+            }
+            for (const auto& kv : members) {
+                const auto& idx = kv.second;
+                for (size_t j = 0; j < idx.size(); j += TC_N) {
+                    TcGroup g;
+                    g.n = kv.first.second;
+                    g.t_off = t_at[kv.first];
+                    g.nbt = static_cast<uint32_t>(
+                        std::min<size_t>(TC_N, idx.size() - j));
+                    g.list_off = static_cast<uint32_t>(tl.size());
+                    tl.insert(tl.end(), idx.begin() + j,
+                              idx.begin() + j + g.nbt);
+                    groups.push_back(g);
+                }
+            }
+            b->tc_groups = static_cast<uint32_t>(groups.size());
+            put(b->tplanes, tp);
+            put(b->tcg, groups);
+            put(b->tclist, tl);
+            VFPS_CUDA(cudaFuncSetAttribute(
+                k_wake_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                static_cast<int>(TC_SMEM)));
+        }
         put(b->row_bunch, row_bunch);
         for (int k = 0; k < 2; k++) {
             b->dens[k].alloc(b->cells);
@@ -1090,7 +1169,7 @@ extern "C" int vfps_batch_info(const vfps_batch* b, uint32_t* launches,
     }
     if (launches) {
         // wake kernel + one map kernel per chain present
-        *launches = 1;
+        *launches = (b->wake_tc && b->tc_groups > 0) ? 2 : 1;
         for (int c = 0; c < TL_COUNT; c++) {
             *launches += b->htiles[c].empty() ? 0 : 1;
         }
@@ -1129,6 +1208,18 @@ extern "C" int vfps_batch_kernel_times(vfps_batch* b, uint32_t nsteps,
         for (int k = 0; k < 3; k++) {
             ms[k] = static_cast<float>(acc[k] / nsteps);
         }
+    });
+}
+
+extern "C" int vfps_batch_set_wake_mode(vfps_batch* b, int mode)
+{
+    if (!b || (mode != 0 && mode != 1)) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    return bguard(b->ctx, [&] {
+        VFPS_CUDA(cudaStreamSynchronize(b->ctx->stream));
+        b->wake_tc = mode;
+        make_graphs(b);
     });
 }
 

@@ -114,7 +114,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         const float* __restrict__ pin, float* __restrict__ wake,
         RowInfo* __restrict__ rinfo, float* __restrict__ factor,
         double* __restrict__ filling, unsigned* __restrict__ counters,
-        int* __restrict__ status)
+        int* __restrict__ status, int wake_ready)
 {
     extern __shared__ float4 wsm4[];
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
@@ -129,7 +129,9 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         P[i] = pin[B.prof_off + i];
     }
     const bool has_wake = B.flags & F_WAKE;
-    if (has_wake) {
+    // wake_ready: the tensor-core kernel has written this step's wake
+    const bool sum_here = has_wake && !wake_ready;
+    if (sum_here) {
         const int nmax = int(B.nmax);
         const float* w = wt + B.wt_off;
         for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
@@ -144,7 +146,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     float* partial = W + 2 * n;          // [Q][n]
     const int G = n >> 2;
     const int Q = G >= THREADS ? 1 : THREADS / G;
-    if (has_wake) {
+    if (sum_here) {
         const int q = threadIdx.x / (THREADS / Q);
         const int span = n / Q;
         const int m0 = q * span;
@@ -176,14 +178,18 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     __syncthreads();
     for (int x = threadIdx.x; x < n; x += THREADS) {
         float v = 0.f;
-        if (has_wake) {
+        if (sum_here) {
             float s = 0.f;
             for (int q = 0; q < Q; q++) {
                 s += partial[size_t(q) * n + x];
             }
             v = __fmul_rn(B.wakescale, s);
+            wake[B.prof_off + x] = v;
+        } else if (has_wake) {
+            v = wake[B.prof_off + x];
+        } else {
+            wake[B.prof_off + x] = 0.f;
         }
-        wake[B.prof_off + x] = v;
         partial[x] = v;    // this thread read partial[.][x] last
     }
     // charge integral (src/PS/PhaseSpace.cpp:200-239) in FP64

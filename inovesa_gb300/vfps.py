@@ -685,10 +685,15 @@ class BunchBatch(_Handle):
                                           C.byref(rows)))
         return launches.value, rows.value
 
+    def set_wake_mode(self, mode):
+        """0: wake potentials on the CUDA cores (default); 1: on the tensor
+        cores (TF32 split products, FP32 accumulation)."""
+        self._check(lib().vfps_batch_set_wake_mode(self._h, int(mode)))
+
     def kernel_times(self, nsteps=20):
         """Advance nsteps steps kernel by kernel; mean ms per step of the
         wake, chain-0 and chain-1 kernels (CUDA events on the library's
         stream)."""
         ms = (C.c_float * 3)()
         self._check(lib().vfps_batch_kernel_times(self._h, nsteps, ms))
-        return {"k_bwake": ms[0], "k_bmaps0": ms[1], "k_bmaps1": ms[2]}
+        return {"wake": ms[0], "k_bmaps0": ms[1], "k_bmaps1": ms[2]}
