@@ -354,6 +354,50 @@ VFPS_API int vfps_batch_kernel_times(vfps_batch* batch, uint32_t nsteps,
  * three products, FP32 accumulation: FP32-level accuracy). */
 VFPS_API int vfps_batch_set_wake_mode(vfps_batch* batch, int mode);
 
+/* ---------------------------------------------------- learned warm start
+ * No counterpart in the reference.  A small network proposes the
+ * equilibrium density of a bunch from (normalised current, gap ratio,
+ * damping time); the proposal enters through vfps_batch_upload (the
+ * PhaseSpace data argument of the reference), and the solver judges it.
+ *   h1 = tanh(W1 x + b1), h2 = tanh(W2 h1 + b2), z = W3 h2 + b3,
+ *   y  = bd + sum_k z_k Wd[k]   (a transposed convolution from a 1x1 map
+ *                                of nlat channels to the npix cells)
+ * In a network the w* point to BF16 weights [out][in] (Wd [nlat][npix]);
+ * in a gradient they point to FP32 arrays of the same shapes.  All
+ * buffers are device memory owned by the caller; nlat must be 32. */
+typedef struct vfps_ws_net {
+    uint32_t nin, nh, nlat, npix;
+    const void* w1;
+    const float* b1;
+    const void* w2;
+    const float* b2;
+    const void* w3;
+    const float* b3;
+    const void* wd;
+    const float* bd;
+} vfps_ws_net;
+/* Forward pass of B samples x[B][nin]: keeps h1, h2 [B][nh] and z
+ * [B][nlat] for the backward pass, writes y [B][npix] if y != NULL.  With
+ * a target [B][npix]: also g = dL/dy of L = sum (y - t)^2 / (B npix), and
+ * partial sums of (y - t)^2 in lpart[nparts] (add them up for the loss). */
+VFPS_API int vfps_ws_forward(vfps_ctx* ctx, const vfps_ws_net* net,
+                             const float* x, uint32_t B, float* h1,
+                             float* h2, float* z, float* y,
+                             const float* target, float* g, double* lpart,
+                             uint32_t nparts);
+/* Backward pass from g = dL/dy: all weight and bias gradients into grad
+ * (FP32), with dz [B][nlat], d1, d2 [B][nh] as workspace. */
+VFPS_API int vfps_ws_backward(vfps_ctx* ctx, const vfps_ws_net* net,
+                              const vfps_ws_net* grad, const float* x,
+                              uint32_t B, const float* h1, const float* h2,
+                              const float* z, const float* g, float* dz,
+                              float* d1, float* d2);
+/* One Adam step (bias-corrected, step >= 1) on FP32 weights w with
+ * moments m, v; writes the BF16 copy w_bf16 when it is not NULL. */
+VFPS_API int vfps_ws_adam(vfps_ctx* ctx, float* w, const float* g, float* m,
+                          float* v, void* w_bf16, size_t count, float lr,
+                          float beta1, float beta2, float eps, uint32_t step);
+
 /* ------------------------------------------------- no-allocation helper
  * No counterpart in the reference.  Charge integral of nb meshes [n][n]
  * that the caller already holds in device memory (density = device

@@ -45,6 +45,16 @@ class BunchDesc(C.Structure):
     ]
 
 
+class WsNet(C.Structure):
+    """Mirror of vfps_ws_net (include/vfps.h)."""
+    _fields_ = [("nin", C.c_uint32), ("nh", C.c_uint32),
+                ("nlat", C.c_uint32), ("npix", C.c_uint32),
+                ("w1", C.c_void_p), ("b1", C.c_void_p),
+                ("w2", C.c_void_p), ("b2", C.c_void_p),
+                ("w3", C.c_void_p), ("b3", C.c_void_p),
+                ("wd", C.c_void_p), ("bd", C.c_void_p)]
+
+
 _lib = None
 P = C.c_void_p
 PP = C.POINTER(C.c_void_p)
@@ -137,6 +147,11 @@ SIGNATURES = {
     "vfps_batch_kernel_times": [P, u32, FP],
     "vfps_charge_noalloc": [P, P, u32, u32, flt, DP],
     "vfps_batch_set_wake_mode": [P, i32],
+    "vfps_ws_forward": [P, C.POINTER(WsNet), P, u32, P, P, P, P, P, P, P,
+                        u32],
+    "vfps_ws_backward": [P, C.POINTER(WsNet), C.POINTER(WsNet), P, u32, P,
+                         P, P, P, P, P, P],
+    "vfps_ws_adam": [P, P, P, P, P, P, sz, flt, flt, flt, flt, u32],
     "vfps_batch_destroy": [P],
 }
 

@@ -1,0 +1,374 @@
+"""Learned warm start: a small network that proposes the equilibrium density
+of a bunch from its normalised current S, gap ratio g/R and damping time
+(in synchrotron periods), trained on equilibria this solver produced.
+
+The proposal enters the solver as initial data (the reference's
+PhaseSpace data argument, inc/PS/PhaseSpace.hpp:54-61, the hook of
+InitialDistFile in src/main.cpp:469-525); the solver stays the judge: a
+bunch counts as converged when the relative L1 change of its profile over
+one synchrotron period falls below a tolerance, and the warm-started and
+the Gaussian-started runs must reach the same equilibrium.
+
+Forward, backward and Adam steps are the library's own kernels
+(vfps_ws_forward / vfps_ws_backward / vfps_ws_adam); PyTorch only holds
+the device buffers.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _lib
+from . import params as P
+from . import vfps as V
+
+NIN, NH, NLAT = 3, 128, 32
+GAP_LO, GAP_HI = 0.004, 0.008
+
+
+def normalise_inputs(S, gap_ratio, damping_periods):
+    """Network inputs, each about unit range over the training domain."""
+    return np.stack([np.asarray(S, np.float64) / 0.25 - 1.0,
+                     (np.asarray(gap_ratio, np.float64) - 0.006) / 0.002,
+                     (np.asarray(damping_periods, np.float64) - 10.0) / 5.0],
+                    axis=-1).astype(np.float32)
+
+
+def bunch_params(n, spt, S, gap_ratio, damping_periods):
+    """Derived parameters of one bunch (parallel-plates CSR impedance)."""
+    base = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+    gap = gap_ratio * base["R_bend"]
+    return P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=gap,
+                    S_csr=float(S), DampingTime=damping_periods / base["fs"])
+
+
+def run_to_equilibrium(ctx, samples, n=256, spt=1000, tol=1e-5,
+                       max_periods=400, start=None):
+    """Advance one batch of bunches period by period until the relative L1
+    change of each profile over a period is below tol.
+
+    samples: (S, gap ratio, damping periods) per bunch; start: optional
+    initial densities [nb][n][n] (else the Gaussian).  Returns (final
+    densities [nb][n][n], periods needed per bunch (-1: not converged))."""
+    zs, keys, descs = {}, [], []
+    for S, g, td in samples:
+        p = bunch_params(n, spt, S, g, td)
+        k = round(float(g), 9)
+        if k not in zs:
+            zs[k] = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+            keys.append(k)
+        descs.append(P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"],
+                                 impedance=keys.index(k)))
+    b = V.BunchBatch(ctx, descs, [zs[k] for k in keys])
+    nb = len(samples)
+    lay = [b.layout(i) for i in range(nb)]
+    if start is not None:
+        full = b.download()
+        for i in range(nb):
+            off = lay[i][0]
+            full[off:off + n * n] = np.asarray(start[i], np.float32).ravel()
+        b.upload(full)
+    done = np.full(nb, -1)
+
+    def profiles():
+        pr = b.profiles()
+        return np.stack([pr[lay[i][1]:lay[i][1] + n] for i in range(nb)])
+
+    prev = profiles()
+    for period in range(1, max_periods + 1):
+        b.step(spt)
+        cur = profiles()
+        change = (np.abs(cur - prev).sum(1)
+                  / np.maximum(np.abs(cur).sum(1), 1e-30))
+        newly = (done < 0) & (change < tol)
+        done[newly] = period
+        prev = cur
+        if np.all(done >= 0):
+            break
+    if ctx.device_status() != 0:
+        raise RuntimeError("device error status during the equilibrium run")
+    full = b.download()
+    dens = np.stack([full[lay[i][0]:lay[i][0] + n * n].reshape(n, n)
+                     for i in range(nb)])
+    return dens, done
+
+
+def simpson_normalise(d, delta):
+    """Scale densities to unit Simpson integral (weights of the reference,
+    src/PS/PhaseSpace.cpp:486-501); negative cells are set to zero."""
+    d = np.maximum(np.asarray(d, np.float64), 0.0)
+    n = d.shape[-1]
+    w = np.full(n, 2.0)
+    w[1::2] = 4.0
+    w[0] = w[-1] = 1.0
+    w *= delta / 3.0
+    integral = np.einsum("...xy,x,y->...", d, w, w)
+    return (d / integral[..., None, None]).astype(np.float32)
+
+
+class WarmStartNet:
+    """The network, its FP32 masters, BF16 copies, gradients and Adam
+    moments, all on one CUDA device."""
+
+    def __init__(self, ctx, npix, seed=0, device=0):
+        import torch
+        self.torch = torch
+        self.ctx = ctx
+        self.npix = int(npix)
+        self.dev = torch.device("cuda", device)
+        rng = np.random.default_rng(seed)
+        shapes = {"w1": (NH, NIN), "b1": (NH,), "w2": (NH, NH), "b2": (NH,),
+                  "w3": (NLAT, NH), "b3": (NLAT,), "wd": (NLAT, self.npix),
+                  "bd": (self.npix,)}
+        self.names = list(shapes)
+        self.w, self.g, self.m, self.v, self.w16 = {}, {}, {}, {}, {}
+        for k, shp in shapes.items():
+            if k.startswith("w"):
+                fan_in = shp[1] if k != "wd" else NLAT
+                init = rng.normal(0.0, 1.0 / math.sqrt(fan_in), size=shp)
+                if k == "wd":
+                    init *= 1e-3
+            else:
+                init = np.zeros(shp)
+            self.w[k] = torch.tensor(init, dtype=torch.float32,
+                                     device=self.dev)
+            self.g[k] = torch.zeros(shp, dtype=torch.float32, device=self.dev)
+            self.m[k] = torch.zeros(shp, dtype=torch.float32, device=self.dev)
+            self.v[k] = torch.zeros(shp, dtype=torch.float32, device=self.dev)
+            if k.startswith("w"):
+                self.w16[k] = self.w[k].to(torch.bfloat16)
+        self.step_count = 0
+        self._ws = {}
+
+    def set_bias(self, mean_density):
+        """Start the decoder from the mean training density."""
+        self.w["bd"].copy_(self.torch.as_tensor(
+            np.asarray(mean_density, np.float32).ravel(), device=self.dev))
+
+    def _net(self, grad=False):
+        src = self.g if grad else None
+        f = {}
+        for k in self.names:
+            if grad:
+                f[k] = src[k].data_ptr()
+            elif k.startswith("w"):
+                f[k] = self.w16[k].data_ptr()
+            else:
+                f[k] = self.w[k].data_ptr()
+        return _lib.WsNet(NIN, NH, NLAT, self.npix, f["w1"], f["b1"],
+                          f["w2"], f["b2"], f["w3"], f["b3"], f["wd"],
+                          f["bd"])
+
+    def _work(self, B):
+        if B not in self._ws:
+            t, d = self.torch, self.dev
+            self._ws[B] = {
+                "h1": t.zeros(B, NH, device=d), "h2": t.zeros(B, NH, device=d),
+                "z": t.zeros(B, NLAT, device=d),
+                "y": t.zeros(B, self.npix, device=d),
+                "g": t.zeros(B, self.npix, device=d),
+                "dz": t.zeros(B, NLAT, device=d),
+                "d1": t.zeros(B, NH, device=d), "d2": t.zeros(B, NH, device=d),
+                "lp": t.zeros(256, dtype=t.float64, device=d)}
+        return self._ws[B]
+
+    def _x(self, x):
+        return self.torch.as_tensor(np.ascontiguousarray(x, np.float32),
+                                    device=self.dev)
+
+    def forward(self, x):
+        """Densities [B][npix] (host) for normalised inputs x [B][3]."""
+        xt = self._x(x)
+        B = xt.shape[0]
+        w = self._work(B)
+        self.torch.cuda.synchronize(self.dev)
+        net = self._net()
+        _lib.check(_lib.lib().vfps_ws_forward(
+            self.ctx.handle, C.byref(net), xt.data_ptr(), B,
+            w["h1"].data_ptr(), w["h2"].data_ptr(), w["z"].data_ptr(),
+            w["y"].data_ptr(), None, None, None, 0), self.ctx.handle)
+        self.ctx.synchronize()
+        return w["y"].cpu().numpy().copy()
+
+    def train_step(self, x, target, lr=1e-3):
+        """One Adam step on a minibatch (target [B][npix] on the device or
+        host); returns the loss."""
+        t = self.torch
+        xt = self._x(x)
+        tt = t.as_tensor(target, dtype=t.float32, device=self.dev)
+        B = xt.shape[0]
+        w = self._work(B)
+        t.cuda.synchronize(self.dev)
+        L = _lib.lib()
+        net, grad = self._net(), self._net(grad=True)
+        nparts = 256
+        _lib.check(L.vfps_ws_forward(
+            self.ctx.handle, C.byref(net), xt.data_ptr(), B,
+            w["h1"].data_ptr(), w["h2"].data_ptr(), w["z"].data_ptr(), None,
+            tt.data_ptr(), w["g"].data_ptr(), w["lp"].data_ptr(), nparts),
+            self.ctx.handle)
+        _lib.check(L.vfps_ws_backward(
+            self.ctx.handle, C.byref(net), C.byref(grad), xt.data_ptr(), B,
+            w["h1"].data_ptr(), w["h2"].data_ptr(), w["z"].data_ptr(),
+            w["g"].data_ptr(), w["dz"].data_ptr(), w["d1"].data_ptr(),
+            w["d2"].data_ptr()), self.ctx.handle)
+        self.step_count += 1
+        for k in self.names:
+            w16 = self.w16[k].data_ptr() if k in self.w16 else None
+            _lib.check(L.vfps_ws_adam(
+                self.ctx.handle, self.w[k].data_ptr(), self.g[k].data_ptr(),
+                self.m[k].data_ptr(), self.v[k].data_ptr(), w16,
+                self.w[k].numel(), lr, 0.9, 0.999, 1e-8, self.step_count),
+                self.ctx.handle)
+        self.ctx.synchronize()
+        return float(w["lp"].sum().item()) / (B * self.npix)
+
+    def gradients(self, x, target):
+        """Loss and gradients (host arrays) without an update (for checks)."""
+        t = self.torch
+        xt = self._x(x)
+        tt = t.as_tensor(target, dtype=t.float32, device=self.dev)
+        B = xt.shape[0]
+        w = self._work(B)
+        t.cuda.synchronize(self.dev)
+        L = _lib.lib()
+        net, grad = self._net(), self._net(grad=True)
+        _lib.check(L.vfps_ws_forward(
+            self.ctx.handle, C.byref(net), xt.data_ptr(), B,
+            w["h1"].data_ptr(), w["h2"].data_ptr(), w["z"].data_ptr(),
+            w["y"].data_ptr(), tt.data_ptr(), w["g"].data_ptr(),
+            w["lp"].data_ptr(), 256), self.ctx.handle)
+        _lib.check(L.vfps_ws_backward(
+            self.ctx.handle, C.byref(net), C.byref(grad), xt.data_ptr(), B,
+            w["h1"].data_ptr(), w["h2"].data_ptr(), w["z"].data_ptr(),
+            w["g"].data_ptr(), w["dz"].data_ptr(), w["d1"].data_ptr(),
+            w["d2"].data_ptr()), self.ctx.handle)
+        self.ctx.synchronize()
+        loss = float(w["lp"].sum().item()) / (B * self.npix)
+        return loss, {k: self.g[k].cpu().numpy().copy() for k in self.names}
+
+    def weights_bf16(self):
+        """The weights the kernels use (BF16 rounded), as float64 arrays."""
+        out = {}
+        for k in self.names:
+            src = self.w16[k] if k in self.w16 else self.w[k]
+            out[k] = src.float().cpu().numpy().astype(np.float64)
+        return out
+
+
+def train(net, x, targets, iters=2000, batch=64, lr=1e-3, seed=1):
+    """Minibatch Adam on (x, targets); cosine-decayed learning rate.
+    Returns the loss history."""
+    rng = np.random.default_rng(seed)
+    t = net.torch
+    tg = t.as_tensor(np.asarray(targets, np.float32).reshape(len(x), -1),
+                     device=net.dev)
+    hist = []
+    for it in range(iters):
+        idx = rng.choice(len(x), size=min(batch, len(x)), replace=False)
+        rate = lr * 0.5 * (1 + math.cos(math.pi * it / iters)) + lr * 1e-3
+        it_idx = t.as_tensor(idx, device=net.dev)
+        hist.append(net.train_step(x[idx], tg[it_idx].contiguous(), rate))
+    return hist
+
+
+def sample_inputs(rng, count, quantise_gap):
+    """(S, gap ratio, damping periods) drawn uniformly from the training
+    domain; training gaps sit on a grid of 9 values (one impedance each)."""
+    S = rng.uniform(0.02, 0.45, size=count)
+    g = rng.uniform(GAP_LO, GAP_HI, size=count)
+    if quantise_gap:
+        g = np.round(g / 0.0005) * 0.0005
+    td = rng.uniform(5.0, 15.0, size=count)
+    return list(zip(S.tolist(), g.tolist(), td.tolist()))
+
+
+def equilibria(ctx, samples, n, spt, tol, max_periods, start=None,
+               chunk=256):
+    dens, done = [], []
+    for i in range(0, len(samples), chunk):
+        d, p = run_to_equilibrium(
+            ctx, samples[i:i + chunk], n=n, spt=spt, tol=tol,
+            max_periods=max_periods,
+            start=None if start is None else start[i:i + chunk])
+        dens.append(d)
+        done.append(p)
+    return np.concatenate(dens), np.concatenate(done)
+
+
+def experiment(ctx, n=256, spt=1000, ntrain=2048, ntest=128, iters=3000,
+               tol=1e-5, max_periods=300, seed=7, log=None, tol_train=None,
+               max_periods_train=None):
+    """Train on solver equilibria, then compare steps to equilibrium from
+    the Gaussian and from the proposal on held-out inputs.  The training
+    equilibria may be converged further than the judging tolerance
+    (tol_train): the stopping rule samples the profile once per
+    synchrotron period and leaves coherent oscillations of about a damping
+    time's worth of the tolerance, which would otherwise be learned as
+    noise."""
+    rng = np.random.default_rng(seed)
+    train_in = sample_inputs(rng, ntrain, True)
+    test_in = sample_inputs(rng, ntest, False)
+    tr_d, tr_p = equilibria(ctx, train_in, n, spt, tol_train or tol,
+                            max_periods_train or max_periods)
+    ok = tr_p >= 0
+    x = normalise_inputs(*np.array(train_in)[ok].T)
+    tgt = tr_d[ok].reshape(int(ok.sum()), -1)
+    net = WarmStartNet(ctx, n * n, seed=seed)
+    net.set_bias(tgt.mean(0))
+    hist = train(net, x, tgt, iters=iters)
+    # held out: Gaussian start, then the proposal
+    g_d, g_p = equilibria(ctx, test_in, n, spt, tol, max_periods)
+    axes = bunch_params(n, spt, *test_in[0])["axes"]
+    dq = (axes[1] - axes[0]) / (n - 1)
+    prop = net.forward(normalise_inputs(*np.array(test_in).T))
+    prop = simpson_normalise(prop.reshape(-1, n, n), dq)
+    w_d, w_p = equilibria(ctx, test_in, n, spt, tol, max_periods, start=prop)
+    both = (g_p > 0) & (w_p > 0)
+    same = np.array([np.abs(w_d[i] - g_d[i]).sum() / np.abs(g_d[i]).sum()
+                     for i in range(ntest)])
+    start_err = np.array([np.abs(prop[i] - g_d[i]).sum()
+                          / np.abs(g_d[i]).sum() for i in range(ntest)])
+    ratio = g_p[both] / np.maximum(w_p[both], 1)
+    out = {
+        "grid": n, "steps_per_period": spt, "tolerance_per_period": tol,
+        "train_tolerance_per_period": tol_train or tol, "iters": iters,
+        "train_samples": int(ntrain), "train_converged": int(ok.sum()),
+        "test_samples": int(ntest), "test_converged_both": int(both.sum()),
+        "test_converged_gaussian": int((g_p > 0).sum()),
+        "test_converged_warm": int((w_p > 0).sum()),
+        "train_loss_first": hist[0], "train_loss_last": hist[-1],
+        "periods_gaussian_median": float(np.median(g_p[both])) if both.any()
+        else None,
+        "periods_warm_median": float(np.median(w_p[both])) if both.any()
+        else None,
+        "speedup_median": float(np.median(ratio)) if both.any() else None,
+        "speedup_total": float(g_p[both].sum() / max(w_p[both].sum(), 1))
+        if both.any() else None,
+        "proposal_l1_median": float(np.median(start_err)),
+        "same_equilibrium_l1_max": float(same[both].max()) if both.any()
+        else None,
+    }
+    if log:
+        log(out)
+    return out, net
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description=experiment.__doc__)
+    ap.add_argument("--grid", type=int, default=256)
+    ap.add_argument("--steps-per-period", type=int, default=1000)
+    ap.add_argument("--train", type=int, default=2048)
+    ap.add_argument("--test", type=int, default=128)
+    ap.add_argument("--iters", type=int, default=3000)
+    ap.add_argument("--train-tol", type=float, default=None)
+    a = ap.parse_args()
+    from . import build as _build
+    _build.build()
+    c = V.Context(0)
+    res, _ = experiment(c, n=a.grid, spt=a.steps_per_period, ntrain=a.train,
+                        ntest=a.test, iters=a.iters, tol_train=a.train_tol,
+                        max_periods_train=600)
+    print(json.dumps(res))
