@@ -249,6 +249,142 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def other_workload(args):
+    """The other workloads of the benchmark plan, one JSON line each (not
+    the headline): plain single bunch (256x256, cubic rotation chain, 500
+    steps per period, free-space CSR, S = 0.05), bursting (512x512,
+    parallel-plates CSR + resistive wall, 4000 steps per period, S = 1.2,
+    CSR power every step), uneven batch (96 seeded bunches of 128..1024,
+    orders 2..4, S ~ U(0.1, 1.5), 2000 steps per period)."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import oracle
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    from inovesa_gb300.solver import PlainSolver
+    ctx = V.Context(0)
+    stream = torch.cuda.ExternalStream(
+        __import__("inovesa_gb300._lib", fromlist=["lib"]).lib().vfps_stream(
+            ctx.handle), device=0)
+    cores = os.cpu_count() or 1
+    out = {"workload": args.workload, "unit": "cell-updates/s",
+           "metric": METRIC}
+
+    def time_plain(s, n, steps, csr=False):
+        s.step(10, csr=csr)
+        ctx.synchronize()
+        t = time.perf_counter()
+        s.step(steps, csr=csr)
+        ctx.synchronize()
+        return n * n * steps / (time.perf_counter() - t)
+
+    def time_oracle(descs, Z, seconds, threads):
+        sim = oracle.Sim(descs, Z=Z, dtype=np.float32)
+        t = time.perf_counter()
+        sim.step(2, threads=threads)
+        per = max((time.perf_counter() - t) / 2, 1e-4)
+        k = max(2, int(seconds / per))
+        t = time.perf_counter()
+        sim.step(k, threads=threads)
+        cells = sum(int(d.n) ** 2 for d in descs) * k
+        return cells / (time.perf_counter() - t), k
+
+    if args.workload in ("plain", "bursting"):
+        if args.workload == "plain":
+            n, spt, chain, S = 256, 500, 1, 0.05
+            fs = P.derive(GridSize=n, StepsPerTs=spt)["fs"]
+            p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                         VacuumGap=-1.0, S_csr=S, DampingTime=100.0 / fs)
+            csr, clamp = False, True
+        else:
+            n, spt, chain, S = 512, 4000, 0, 1.2
+            p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+            p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                         VacuumGap=0.006 * p0["R_bend"], S_csr=S,
+                         WallConductivity=5.8e7)
+            csr, clamp = True, False
+        z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+        zr = (V.makeImpedance(ctx, **P.csr_impedance_args(p)) if csr
+              else None)
+        s = PlainSolver(ctx, p, chain=chain, wake_impedance=z,
+                        csr_impedance=zr, it=4, clamp=clamp)
+        out["gpu_plain"] = time_plain(s, n, args.steps, csr)
+        d = P.fill_desc(oracle.BunchDesc(), p, chain, Ib=p["Ib"], it=4,
+                        clamp=clamp)
+        v1, k1 = time_oracle([d], z.data(), 10.0, 1)
+        out["cpu_1core"] = v1
+        out["cpu_sample"] = "%d solver steps of the bunch, 1 thread" % k1
+        # accuracy of the plain GPU loop against FP64 over 2 periods
+        s2 = PlainSolver(ctx, p, chain=chain, wake_impedance=z, it=4,
+                         clamp=clamp)
+        ref = oracle.Sim([d], Z=z.data(), dtype=np.float64)
+        steps = 2 * spt if args.workload == "plain" else 200
+        s2.step(steps)
+        ref.step(steps)
+        want = ref.density(0)
+        out["density_l1_vs_fp64"] = float(
+            np.abs(s2.density() - want).sum() / np.abs(want).sum())
+        out["accuracy_steps"] = steps
+        out["config"] = {"grid": n, "steps_per_period": spt, "S": S,
+                         "chain": chain, "csr_every_step": csr}
+    else:
+        rng = np.random.default_rng(4)
+        nb, spt = 96, 2000
+        sizes = rng.choice([128, 256, 512, 1024], size=nb)
+        cur = rng.uniform(0.1, 1.5, size=nb)
+        its = rng.choice([2, 3, 4], size=nb)
+        keys = sorted(set(int(v) for v in sizes))
+        zs = {}
+        for k in keys:
+            p0 = P.derive(GridSize=k, StepsPerTs=spt, padding=2.0)
+            pk = P.derive(GridSize=k, StepsPerTs=spt, padding=2.0,
+                          VacuumGap=0.006 * p0["R_bend"])
+            zs[k] = V.makeImpedance(ctx, **P.wake_impedance_args(pk))
+        descs, ps = [], []
+        for n, S, it in zip(sizes, cur, its):
+            n, it = int(n), int(it)
+            p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+            p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                         VacuumGap=0.006 * p0["R_bend"], S_csr=float(S))
+            ps.append((p, it))
+            descs.append(P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"],
+                                     impedance=keys.index(n), it=it))
+        b = V.BunchBatch(ctx, descs, [zs[k] for k in keys])
+        b.step(args.warmup)
+        ctx.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out["gpu_batched"] = b.cells * args.steps / (ms / 1e3)
+        out["kernel_ms_per_step"] = b.kernel_times(20)
+        out["cells_per_step"] = int(sum(int(v) ** 2 for v in sizes))
+        # the plain loop, one bunch at a time, on one bunch of each size
+        rates = []
+        for k in keys:
+            i = int(np.nonzero(sizes == k)[0][0])
+            p, it = ps[i]
+            s = PlainSolver(ctx, p, chain=0, wake_impedance=zs[k], it=it)
+            rates.append((k, time_plain(s, k, 200)))
+        # whole batch one bunch after another at those rates
+        t_plain = sum(int(n) ** 2 / dict(rates)[int(n)] for n in sizes)
+        out["gpu_plain"] = out["cells_per_step"] / t_plain
+        od = [P.fill_desc(oracle.BunchDesc(), p, 0, Ib=p["Ib"], it=it)
+              for p, it in ps[:max(cores, 1)]]
+        vv, kk = time_oracle(od, None, 12.0, cores)
+        out["cpu_all_cores"] = vv
+        out["cpu_cores"] = cores
+        out["cpu_sample"] = ("%d bunches of the batch, %d steps, no wake, "
+                             "%d threads" % (len(od), kk, cores))
+        out["config"] = {"bunches": nb, "sizes": "seeded 128..1024",
+                         "steps_per_period": spt}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -257,6 +393,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="scan",
+                    choices=["scan", "plain", "bursting", "uneven"],
+                    help="scan: the headline line; the others print one "
+                         "line of their own")
     ap.add_argument("--wake-mode", type=int, default=0, choices=[0, 1],
                     help="wake potentials on the CUDA cores (0) or the "
                          "tensor cores (1); the other mode is measured "
@@ -270,6 +410,9 @@ def main():
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "scan":
+        other_workload(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))
