@@ -8,7 +8,11 @@ from . import vfps as V
 
 class PlainSolver:
     def __init__(self, ctx, p, chain=0, Ib=None, wake_impedance=None,
-                 csr_impedance=None, it=None, clamp=False, data=None):
+                 csr_impedance=None, it=None, clamp=False, data=None,
+                 resume_step=None):
+        """data: initial density [n][n] (else the Gaussian); with
+        resume_step, data is a saved state that continues at that step
+        (not normalised again, renormalisation schedule kept)."""
         o = p["opts"]
         self.p, self.chain = p, chain
         n = p["ps_bins"]
@@ -19,9 +23,11 @@ class PlainSolver:
         self.t1 = V.PhaseSpace(a[0], a[1], a[2], a[3], a[4], a[5], ctx,
                                ib / p["f_rev"], ib, [1.0],
                                o["InitialDistZoom"], data, n=n)
-        if self.renormalize >= 0:
+        if self.renormalize >= 0 and resume_step is None:
             self.t1.updateXProjection()
             self.t1.normalize()
+        elif resume_step is not None:
+            self.t1.updateXProjection()
         self.t2 = self.t1.copy()
         self.t3 = self.t1.copy()
         self.wake_field = None
@@ -66,7 +72,7 @@ class PlainSolver:
         if csr_impedance is not None:
             self.rdtn = V.ElectricField(self.t1, csr_impedance, [0], 0, ctx,
                                         p["f_rev"], p["revolutionpart"])
-        self.simulationstep = 0
+        self.simulationstep = 0 if resume_step is None else int(resume_step)
 
     def step(self, nsteps=1, csr=False):
         for _ in range(nsteps):
