@@ -169,6 +169,29 @@ VFPS_API int vfps_rf_kick_map_create(vfps_ps* in, vfps_ps* out,
                                      float revolutionpart, float v_rf,
                                      float f_rf, float v0, int it, int clamp,
                                      vfps_map** map);
+/* DynamicRFKickMap (src/SM/DynamicRFKickMap.cpp:15-109): an RF kick map
+ * whose phase and amplitude change at every apply, phase = syncphase +
+ * N(0,1) phasespread/sqrt(revolutionpart) + modampl sin(2 pi
+ * modtimeincrement i), amplitude = 1 + N(0,1) amplspread/sqrt(
+ * revolutionpart) for apply number i; linear = 1 uses the linear RF
+ * (angle), 0 the sinusoidal RF (v_rf, v0).  The normals come from a
+ * counter-based generator (Philox-4x32-10 keyed by seed, Box-Muller), so a
+ * run is reproducible (the reference seeds std::mt19937 from
+ * std::random_device).  The first `steps` modulations are logged for
+ * vfps_dynamic_rf_get_modulation (the reference's getPastModulation). */
+VFPS_API int vfps_dynamic_rf_kick_map_create(
+    vfps_ps* in, vfps_ps* out, int linear, float angle, float revolutionpart,
+    float v_rf, float f_rf, float v0, float phasespread, float amplspread,
+    float modampl, double modtimeincrement, uint32_t steps, int it,
+    int clamp, uint32_t seed, vfps_map** map);
+/* out[2*count] = (phase, amplitude) of the applies so far (at most the
+ * logged `steps`); either pointer may be NULL. */
+VFPS_API int vfps_dynamic_rf_get_modulation(vfps_map* map, float* out,
+                                            uint64_t* count);
+/* The generator of the dynamic RF map (no counterpart in the reference):
+ * Philox-4x32-10 of counter[4] under key[2] into out[4]. */
+VFPS_API int vfps_philox4x32(const uint32_t* counter, const uint32_t* key,
+                             uint32_t* out);
 /* FokkerPlanckMap(in,out,xsize,ysize,fptype,fptrack,e1,derivation,oclh),
  * inc/SM/FokkerPlanckMap.hpp:56-64 */
 VFPS_API int vfps_fokker_planck_map_create(vfps_ps* in, vfps_ps* out,

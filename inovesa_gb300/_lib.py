@@ -101,6 +101,11 @@ SIGNATURES = {
     "vfps_drift_map_create": [P, P, FP, u32, flt, i32, i32, PP],
     "vfps_rf_kick_map_create_linear": [P, P, flt, flt, i32, i32, PP],
     "vfps_rf_kick_map_create": [P, P, flt, flt, flt, flt, i32, i32, PP],
+    "vfps_dynamic_rf_kick_map_create": [P, P, i32, flt, flt, flt, flt, flt,
+                                        flt, flt, flt, dbl, u32, i32, i32,
+                                        u32, PP],
+    "vfps_dynamic_rf_get_modulation": [P, FP, C.POINTER(C.c_uint64)],
+    "vfps_philox4x32": [U32P, U32P, U32P],
     "vfps_fokker_planck_map_create": [P, P, u32, u32, i32, i32, flt, i32, PP],
     "vfps_identity_map_create": [P, P, PP],
     "vfps_wake_potential_map_create": [P, P, P, i32, i32, PP],

@@ -792,6 +792,75 @@ extern "C" int vfps_rf_kick_map_create(vfps_ps* in, vfps_ps* out,
     });
 }
 
+extern "C" int vfps_dynamic_rf_kick_map_create(
+    vfps_ps* in, vfps_ps* out, int linear, float angle, float revolutionpart,
+    float v_rf, float f_rf, float v0, float phasespread, float amplspread,
+    float modampl, double modtimeincrement, uint32_t steps, int it,
+    int clamp, uint32_t seed, vfps_map** map)
+{
+    if (!in || !out || !map) {
+        return null_arg("in/out/map");
+    }
+    *map = nullptr;
+    return guard(in->ctx, [&] {
+        VFPS_REQUIRE(revolutionpart > 0, "revolutionpart must be positive");
+        VFPS_REQUIRE(linear || (v_rf != 0 && std::fabs(v0) <= std::fabs(v_rf)),
+                     "sinusoidal RF needs |V0| <= |V_RF| != 0");
+        auto m = new_kick(in, out, it, clamp, VFPS_AXIS_Y);
+        const vfps::Axis& ax = in->ax[0];
+        DynRf& d = m->dyn;
+        d.linear = linear ? 1 : 0;
+        d.angle = angle;
+        d.revolutionpart = revolutionpart;
+        d.v_rf = v_rf;
+        d.v0 = v0;
+        // src/SM/RFKickMap.cpp:15-57
+        d.syncphase = linear ? 0.f : std::asin(v0 / v_rf);
+        d.bl2phase = static_cast<float>(double(ax.scale) / C_LIGHT
+                                        * double(f_rf) * 2 * PI);
+        // src/SM/DynamicRFKickMap.cpp:31-38
+        d.phasenoise = phasespread / std::sqrt(revolutionpart);
+        d.amplnoise = amplspread / std::sqrt(revolutionpart);
+        d.modampl = modampl;
+        d.modtimedelta = 2 * PI * modtimeincrement;
+        d.seed = seed;
+        m->dynrf = true;
+        m->dyn_cap = steps;
+        m->dyn_log.alloc(std::max<size_t>(2 * size_t(steps), 2));
+        m->axis_q.alloc(in->n);
+        h2d(m->axis_q.p, ax.v.data(), in->n, in->ctx);
+        m->host_offset_valid = false;
+        *map = m.release();
+    });
+}
+
+extern "C" int vfps_dynamic_rf_get_modulation(vfps_map* map, float* out,
+                                              uint64_t* count)
+{
+    if (!map || !map->dynrf) {
+        return null_arg("map (a dynamic RF kick map)");
+    }
+    return guard(map->in->ctx, [&] {
+        const uint64_t c = std::min(map->dyn_step, map->dyn_cap);
+        if (count) {
+            *count = c;
+        }
+        if (out && c) {
+            d2h(out, map->dyn_log.p, 2 * c, map->in->ctx);
+        }
+    });
+}
+
+extern "C" int vfps_philox4x32(const uint32_t* counter, const uint32_t* key,
+                               uint32_t* out)
+{
+    if (!counter || !key || !out) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    philox4x32_10(counter, key, out);
+    return VFPS_OK;
+}
+
 extern "C" int vfps_fokker_planck_map_create(vfps_ps* in, vfps_ps* out,
                                              uint32_t xsize, uint32_t ysize,
                                              int fptype, int fptrack, float e1,
@@ -978,6 +1047,10 @@ extern "C" int vfps_map_apply(vfps_map* map)
             vfps::launch_rotation(map);
             break;
         case MAP_KICK:
+            if (map->dynrf) {
+                vfps::launch_dynrf(map);
+                map->host_offset_valid = false;
+            }
             vfps::launch_kick(map, map->field ? map->offset_src
                                               : map->offset.p);
             break;

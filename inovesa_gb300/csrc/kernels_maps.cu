@@ -139,7 +139,73 @@ __global__ void k_fp(const float* __restrict__ in, float* __restrict__ out,
     out[row + y] = value;
 }
 
+// DynamicRFKickMap::apply (src/SM/DynamicRFKickMap.cpp:79-109 and
+// RFKickMap::_calcKick, src/SM/RFKickMap.cpp:59-83): the modulation of
+// apply number `step` -- phase = syncphase + N(0,1) phasenoise + modampl
+// sin(2 pi modtimeincrement step), amplitude = 1 + N(0,1) amplnoise, the
+// normals drawn by Box-Muller from Philox(step, seed) -- and the RF kick
+// offsets of every row with it (identical for every bunch).
+__global__ void k_dynrf(DynRf d, uint64_t step, const float* __restrict__ q,
+                        float xcenter, float dq, float dp, float pscale,
+                        uint32_t n, uint32_t nb, float* __restrict__ offset,
+                        float* __restrict__ log)
+{
+    const uint32_t ctr[4] = {uint32_t(step), uint32_t(step >> 32), 0u, 0u};
+    const uint32_t key[2] = {d.seed, 0x5EED0001u};
+    uint32_t r[4];
+    philox4x32_10(ctr, key, r);
+    // uniforms in (0, 1]
+    const float u1 = (float(r[0] >> 8) + 1.f) * (1.f / 16777216.f);
+    const float u2 = (float(r[1] >> 8) + 1.f) * (1.f / 16777216.f);
+    const float rad = sqrtf(-2.f * logf(u1));
+    float sn, cs;
+    sincospif(2.f * u2, &sn, &cs);
+    const float n1 = rad * cs, n2 = rad * sn;
+    const float mod = d.modampl
+        * static_cast<float>(sin(d.modtimedelta * double(step)));
+    const float phase = d.syncphase + n1 * d.phasenoise + mod;
+    const float ampl = 1.f + n2 * d.amplnoise;
+    if (blockIdx.x == 0 && threadIdx.x == 0 && log) {
+        log[0] = phase;
+        log[1] = ampl;
+    }
+    for (uint32_t x = blockIdx.x * blockDim.x + threadIdx.x; x < n;
+         x += gridDim.x * blockDim.x) {
+        float o;
+        if (d.linear) {
+            const float phaseoffs = d.syncphase - phase;
+            const float ta = tanf(d.angle);
+            o = __fmul_rn(ta, __fsub_rn(xcenter, float(x)));
+            o = __fadd_rn(o, __fdiv_rn(__fdiv_rn(__fmul_rn(ta, phaseoffs),
+                                                 d.bl2phase), dq));
+            o = __fmul_rn(o, ampl);
+        } else {
+            const float arg = __fadd_rn(__fmul_rn(q[x], d.bl2phase), phase);
+            const float v = __fadd_rn(__fmul_rn(-ampl * d.v_rf, sinf(arg)),
+                                      d.v0);
+            o = __fdiv_rn(__fdiv_rn(__fmul_rn(d.revolutionpart, v), dp),
+                          pscale);
+        }
+        for (uint32_t b = 0; b < nb; b++) {
+            offset[size_t(b) * n + x] = o;
+        }
+    }
+}
+
 }  // namespace
+
+void launch_dynrf(vfps_map* m)
+{
+    const vfps_ps* in = m->in;
+    const uint32_t n = in->n;
+    float* log = m->dyn_step < m->dyn_cap ? m->dyn_log.p + 2 * m->dyn_step
+                                          : nullptr;
+    k_dynrf<<<(n + 127) / 128, 128, 0, in->ctx->stream>>>(
+        m->dyn, m->dyn_step, m->axis_q.p, in->ax[0].zerobin, in->ax[0].delta,
+        in->ax[1].delta, in->ax[1].scale, n, in->nb, m->offset.p, log);
+    VFPS_LAUNCHED();
+    m->dyn_step++;
+}
 
 void launch_rotation(const vfps_map* m)
 {

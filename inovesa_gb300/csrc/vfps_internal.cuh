@@ -131,6 +131,45 @@ enum MapKind {
     MAP_IDENTITY
 };
 
+// Counter-based generator Philox-4x32-10 (Salmon, Moraes, Dror, Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC 2011): ten rounds of
+// two 32x32->64-bit multiplications mixing a 128-bit counter under a
+// 64-bit key bumped by the Weyl constants between rounds.
+__host__ __device__ inline void philox4x32_10(const uint32_t ctr[4],
+                                              const uint32_t key[2],
+                                              uint32_t out[4])
+{
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; r++) {
+        const uint64_t p0 = uint64_t(0xD2511F53u) * c0;
+        const uint64_t p1 = uint64_t(0xCD9E8D57u) * c2;
+        const uint32_t hi0 = uint32_t(p0 >> 32), lo0 = uint32_t(p0);
+        const uint32_t hi1 = uint32_t(p1 >> 32), lo1 = uint32_t(p1);
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0;
+    out[1] = c1;
+    out[2] = c2;
+    out[3] = c3;
+}
+
+// parameters of a DynamicRFKickMap (src/SM/DynamicRFKickMap.cpp:15-109)
+struct DynRf {
+    int linear = 1;
+    float angle = 0, revolutionpart = 0, v_rf = 0, v0 = 0;
+    float syncphase = 0, bl2phase = 0;
+    float phasenoise = 0, amplnoise = 0;   // spreads / sqrt(revolutionpart)
+    float modampl = 0;
+    double modtimedelta = 0;               // 2 pi modtimeincrement
+    uint32_t seed = 0;
+};
+
 struct vfps_map {
     MapKind kind = MAP_IDENTITY;
     int device = 0;
@@ -147,6 +186,13 @@ struct vfps_map {
     vfps_field* field = nullptr;
     std::vector<float> host_offset;  // mirror for applyTo / getForce
     bool host_offset_valid = true;
+    // DynamicRFKickMap: per-step phase and amplitude drawn on the device
+    bool dynrf = false;
+    DynRf dyn;
+    uint64_t dyn_step = 0;                 // applies so far
+    vfps::DevBuf<float> dyn_log;           // [capacity][2] phase, ampl
+    uint64_t dyn_cap = 0;
+    vfps::DevBuf<float> axis_q;            // q axis values [n]
     // Fokker-Planck
     int ip = 0;
     int fptrack = 0;
@@ -206,6 +252,7 @@ void launch_moments(vfps_ps* ps, int axis);
 
 void launch_rotation(const vfps_map* m);
 void launch_kick(const vfps_map* m, const float* offset);
+void launch_dynrf(vfps_map* m);
 void launch_fp(const vfps_map* m);
 
 void launch_wake_table(vfps_field* f);

@@ -17,7 +17,7 @@ from ._lib import BunchDesc, InvalidArgument, VfpsError, check, lib
 
 __all__ = [
     "Context", "PhaseSpace", "RotationMap", "KickMap", "DriftMap",
-    "RFKickMap", "FokkerPlanckMap", "Identity", "WakePotentialMap",
+    "RFKickMap", "DynamicRFKickMap", "FokkerPlanckMap", "Identity", "WakePotentialMap",
     "Impedance", "FreeSpaceCSR", "ParallelPlatesCSR", "ResistiveWall",
     "ConstImpedance", "CollimatorImpedance", "makeImpedance",
     "ElectricField", "BunchBatch", "BunchDesc", "InvalidArgument",
@@ -367,6 +367,45 @@ class RFKickMap(KickMap):
         h = _new_map(lib().vfps_rf_kick_map_create, grid_in, grid_out.handle,
                      revolutionpart, V_RF, f_RF, V0, it, int(interpol_clamp))
         return cls(grid_in, grid_out, 0, 0, it, interpol_clamp, _handle=h)
+
+
+class DynamicRFKickMap(KickMap):
+    """DynamicRFKickMap(in, out, angle, revolutionpart, f_RF, phasespread,
+    amplspread, modampl, modtimeincrement, steps, it, clamp) -- linear RF;
+    DynamicRFKickMap.sinusoidal(in, out, revolutionpart, V_RF, f_RF, V0,
+    ...) for the sinusoidal one.  ``seed`` keys the counter-based
+    generator of the phase and amplitude noise."""
+
+    def __init__(self, grid_in, grid_out, angle, revolutionpart, f_RF,
+                 phasespread, amplspread, modampl, modtimeincrement, steps,
+                 it, interpol_clamp, oclh=None, seed=0, _linear=True,
+                 _v_rf=0.0, _v0=0.0):
+        h = _new_map(lib().vfps_dynamic_rf_kick_map_create, grid_in,
+                     grid_out.handle, int(_linear), angle, revolutionpart,
+                     _v_rf, f_RF, _v0, phasespread, amplspread, modampl,
+                     modtimeincrement, steps, it, int(interpol_clamp), seed)
+        super().__init__(grid_in, grid_out, it, interpol_clamp, Axis.y,
+                         _handle=h)
+
+    @classmethod
+    def sinusoidal(cls, grid_in, grid_out, revolutionpart, V_RF, f_RF, V0,
+                   phasespread, amplspread, modampl, modtimeincrement, steps,
+                   it, interpol_clamp, oclh=None, seed=0):
+        return cls(grid_in, grid_out, 0.0, revolutionpart, f_RF,
+                   phasespread, amplspread, modampl, modtimeincrement, steps,
+                   it, interpol_clamp, oclh, seed, _linear=False,
+                   _v_rf=V_RF, _v0=V0)
+
+    def getPastModulation(self):
+        """[(phase, amplitude)] of the applies so far (as logged)."""
+        c = C.c_uint64()
+        self._check(lib().vfps_dynamic_rf_get_modulation(self._h, None,
+                                                         C.byref(c)))
+        out = np.empty((c.value, 2), np.float32)
+        if c.value:
+            self._check(lib().vfps_dynamic_rf_get_modulation(
+                self._h, _fptr(out), C.byref(c)))
+        return out
 
 
 class FokkerPlanckMap(SourceMap):
