@@ -1098,9 +1098,14 @@ extern "C" int vfps_map_apply_to(vfps_map* map, float* pos, size_t count)
         case MAP_KICK: {
             // src/SM/KickMap.cpp:280-303 (offsets of bunch 0)
             if (!map->host_offset_valid) {
-                map->host_offset.resize(map->field->wake.n);
-                d2h(map->host_offset.data(), map->field->wake.p,
-                    map->field->wake.n, ps->ctx);
+                // the wake map's offsets live in its field, the others' in
+                // the map (the dynamic RF map rewrites them every apply)
+                const float* src = map->field ? map->field->wake.p
+                                              : map->offset.p;
+                const size_t cnt = map->field ? map->field->wake.n
+                                              : map->offset.n;
+                map->host_offset.resize(cnt);
+                d2h(map->host_offset.data(), src, cnt, ps->ctx);
                 map->host_offset_valid = true;
             }
             const auto& off = map->host_offset;

@@ -98,3 +98,21 @@ def test_noise_statistics_and_seed(gpu_ctx):
     assert abs(np.corrcoef(m[:, 0], m[:, 1])[0, 1]) < 0.1
     assert np.array_equal(runs[0], runs[1])
     assert not np.array_equal(runs[0], runs[2])
+
+
+def test_particles_follow_the_dynamic_kick(gpu_ctx):
+    """applyTo of a dynamic map uses the offsets of its last apply (the
+    reference's KickMap::applyTo, src/SM/KickMap.cpp:280-303)."""
+    p, g1, g2 = grids(gpu_ctx)
+    o1, o2 = g1.copy(), g2.copy()
+    st = V.RFKickMap(g1, o1, p["angle"], p["f_RF"], 4, False)
+    dy = V.DynamicRFKickMap(g2, o2, p["angle"], p["revolutionpart"],
+                            p["f_RF"], 0.0, 0.0, 0.0, 0.0, 4, 4, False)
+    st.apply()
+    dy.apply()
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(10, 110, size=(50, 2)).astype(np.float32)
+    a = st.applyToAll(pts)
+    b = dy.applyToAll(pts)
+    assert np.allclose(a, b, rtol=0, atol=1e-4)
+    assert np.abs(a - pts).max() > 0

@@ -211,3 +211,31 @@ def test_wake_and_csr(gpu_ctx, gap):
                                P.C / p["bl"])
     assert np.max(np.abs(spec - rspec)) <= 1e-5 * np.abs(rspec).max()
     assert abs(power - rpower) <= 1e-5 * abs(rpower)
+
+
+def test_multi_bucket_wake(gpu_ctx):
+    """Bunches of one beam in buckets 0, 2 and 5 share the padded profile
+    (src/PS/ElectricField.cpp:186-263): each bunch's wake carries the
+    other bunches' fields at their bucket distance."""
+    n, nb = 64, 3
+    buckets = [0, 2, 5]
+    p = P.derive(GridSize=n, padding=16.0, VacuumGap=0.0318, S_csr=0.5)
+    spacing = 3 * n // 2
+    rng = np.random.default_rng(9)
+    d = rng.random((nb, n, n)).astype(np.float32)
+    ps = V.PhaseSpace(*p["axes"], gpu_ctx, 1, 1, [0.5, 0.3, 0.2], 1.0, d,
+                      n=n)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    f = V.ElectricField.wake(ps, z, buckets, spacing, gpu_ctx, p["f_rev"],
+                             p["revolutionpart"], p["Ib"], p["E0"], p["sE"],
+                             p["dt"])
+    ps.updateXProjection()
+    wake = f.wakePotential()
+    proj = ps.getProjection(0)
+    ref = oracle.wake_potential(proj, z.data(), float(np.float32(
+        p["wakescaling"])), buckets=buckets, spacing=spacing)
+    assert np.max(np.abs(wake - ref)) <= 1e-5 * np.abs(ref).max()
+    # the coupling is there: without the other bunches the wake differs
+    alone = oracle.wake_potential(proj[:1], z.data(), float(np.float32(
+        p["wakescaling"])))[0]
+    assert np.abs(alone - ref[0]).max() > 1e-3 * np.abs(ref[0]).max()
