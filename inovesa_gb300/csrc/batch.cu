@@ -58,7 +58,8 @@ struct vfps_batch {
     DevBuf<float> wake, factor;
     DevBuf<RowInfo> rinfo;     // chain-0 y-kick stencils of every row
     DevBuf<double> filling;
-    DevBuf<unsigned> counters;
+    // step tickets: every k_bwake CTA takes one, so step = tickets / nb
+    DevBuf<unsigned long long> tickets;
     int cur = 0;               // buffer holding the current state
     size_t smem[TL_COUNT] = {0, 0, 0};
     SmemR layoutR{};           // shared-memory regions of k_bmaps0
@@ -155,9 +156,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             VFPS_CUDA(cudaEventRecord(ev[i], st));
         }
     };
-    // P[n], W[2n], partial sums [Q][n] with Q n <= max(1024, n)
-    const size_t wsm = (3 * size_t(b->max_n)
-                        + std::max<size_t>(1024, b->max_n)) * sizeof(float);
+    // P[n], W[2n], partial sums [Q][n] with Q n = 8 THREADS
+    const size_t wsm = (3 * size_t(b->max_n) + 8 * THREADS) * sizeof(float);
     mark(0);
     const bool tc = b->wake_tc && b->tc_groups > 0;
     if (tc) {
@@ -169,16 +169,32 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     }
     k_bwake<<<b->nb, THREADS, wsm, st>>>(
         b->bd.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p, b->wake.p,
-        b->rinfo.p, b->factor.p, b->filling.p, b->counters.p,
+        b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p,
         b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
     if (!b->htiles[TL_RING].empty()) {
-        k_bmaps0<<<b->gridR, RTHREADS, b->smem[TL_RING], st>>>(
-            b->bd.p, b->tiles[TL_RING].p,
-            static_cast<uint32_t>(b->htiles[TL_RING].size()), b->tabs.p,
-            b->dwt.p, b->rinfo.p, b->dens[from].p, b->dens[to].p,
-            b->prof[to].p, b->ctx->d_status, b->layoutR);
+        // programmatic dependent launch: the CTAs zero their rings and set
+        // up their barriers while k_bwake runs, then wait for it to finish
+        // (griddepcontrol.wait) before they read or write device memory.
+        // Only this kernel is launched so: k_bwake CTAs launched early
+        // crowd onto the SMs that finish this kernel first, which is slower.
+        cudaLaunchAttribute pdl[1];
+        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t c = {};
+        c.gridDim = dim3(b->gridR);
+        c.blockDim = dim3(RTHREADS);
+        c.dynamicSmemBytes = b->smem[TL_RING];
+        c.stream = st;
+        c.attrs = pdl;
+        c.numAttrs = 1;
+        VFPS_CUDA(cudaLaunchKernelEx(
+            &c, k_bmaps0, (const BDev*)b->bd.p, (const Tile*)b->tiles[TL_RING].p,
+            static_cast<uint32_t>(b->htiles[TL_RING].size()),
+            (const float*)b->tabs.p, (const float*)b->dwt.p,
+            (const RowInfo*)b->rinfo.p, (const float*)b->dens[from].p,
+            b->dens[to].p, b->prof[to].p, b->ctx->d_status, b->layoutR));
         VFPS_LAUNCHED();
     }
     if (!b->htiles[TL_WIDE].empty()) {
@@ -409,8 +425,8 @@ int autotune(vfps_batch* b)
                               cudaMemcpyDeviceToDevice, st));
     VFPS_CUDA(cudaMemcpyAsync(sp.p, b->prof[b->cur].p, sp.bytes(),
                               cudaMemcpyDeviceToDevice, st));
-    unsigned saved[2];
-    VFPS_CUDA(cudaMemcpyAsync(saved, b->counters.p, sizeof(saved),
+    unsigned long long saved = 0;
+    VFPS_CUDA(cudaMemcpyAsync(&saved, b->tickets.p, sizeof(saved),
                               cudaMemcpyDeviceToHost, st));
     VFPS_CUDA(cudaStreamSynchronize(st));
     const int cands[] = {2048, 3072, 4096, 6144, 8192, 12288};
@@ -450,7 +466,7 @@ int autotune(vfps_batch* b)
                               cudaMemcpyDeviceToDevice, st));
     VFPS_CUDA(cudaMemcpyAsync(b->prof[b->cur].p, sp.p, sp.bytes(),
                               cudaMemcpyDeviceToDevice, st));
-    VFPS_CUDA(cudaMemcpyAsync(b->counters.p, saved, sizeof(saved),
+    VFPS_CUDA(cudaMemcpyAsync(b->tickets.p, &saved, sizeof(saved),
                               cudaMemcpyHostToDevice, st));
     VFPS_CUDA(cudaStreamSynchronize(st));
     {
@@ -919,8 +935,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         VFPS_CUDA(cudaMemsetAsync(b->wake.p, 0, b->wake.bytes(), st));
         b->factor.alloc(nb);
         b->filling.alloc(nb);
-        b->counters.alloc(2);
-        VFPS_CUDA(cudaMemsetAsync(b->counters.p, 0, b->counters.bytes(), st));
+        b->tickets.alloc(1);
+        VFPS_CUDA(cudaMemsetAsync(b->tickets.p, 0, b->tickets.bytes(), st));
         b->cur = 0;
         if (data) {
             size_t src = 0;

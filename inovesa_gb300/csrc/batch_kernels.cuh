@@ -3,7 +3,7 @@
 //  k_bwake   one CTA per bunch: the wake potential of every mesh row as
 //            the Toeplitz sum  wake[x] = s sum_m P[m] w[(x-m) mod nmax]  of
 //            the previous step's profile P (w built once per impedance in
-//            FP64), the charge integral (FP64), this step's
+//            FP64), the charge integral (compensated FP32), this step's
 //            renormalisation factor and the step counter.
 //  k_bmaps0  chain 0 (the reference's loop, src/main.cpp:1034-1044) for
 //            meshes up to 256 rows: a persistent kernel whose CTAs walk
@@ -108,23 +108,57 @@ __device__ __forceinline__ RowStencil make_stencil(float offset, uint32_t n,
 }
 
 // ----------------------------------------------------------------- wake
+// Compensated FP32 sums (float-float: value = hi + lo).  A product of two
+// floats splits exactly into hi + lo with one FMA; additions use Knuth's
+// two-sum, whose error term is exact, so a + b and b + a give the same
+// bits.  About 48 significant bits: far finer than the reference's FP32
+// charge integral, and on this GPU much cheaper than FP64 arithmetic.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF ff_prod(float a, float b)
+{
+    const float p = __fmul_rn(a, b);
+    return FF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ FF ff_add(FF a, FF b)
+{
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float v = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, e);
+    return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+
+// One CTA per bunch: wake potential of the previous step's profile, charge
+// integral, renormalisation factor and, for chain 0, both y-kick stencils
+// of every row.  The step number comes from a 64-bit ticket that every CTA
+// takes once per step (nb tickets per step), so no CTA has to wait for the
+// others or reset anything.
 __global__ void __launch_bounds__(THREADS)
 k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         const float* __restrict__ wt, const RowStencil* __restrict__ st,
         const float* __restrict__ pin, float* __restrict__ wake,
         RowInfo* __restrict__ rinfo, float* __restrict__ factor,
-        double* __restrict__ filling, unsigned* __restrict__ counters,
+        double* __restrict__ filling, unsigned long long* __restrict__ tickets,
         int* __restrict__ status, int wake_ready)
 {
     extern __shared__ float4 wsm4[];
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
-    __shared__ double red[32];
-    __shared__ float fac_s;
+    __shared__ float2 red[32];
+    __shared__ unsigned long long ticket_s;
+    // the maps kernel that follows may start its prologue now
+    pdl_trigger();
     const uint32_t b = blockIdx.x;
     const BDev B = bd[b];
     const int n = int(B.n);
     float* W = P + n;   // W[k] = w[(k - (n-1)) mod nmax], k < 2n - 1
-    const unsigned step = *((volatile unsigned*)counters);
+    if (threadIdx.x == 0) {
+        ticket_s = atomicAdd(tickets, 1ull);
+    }
     for (int i = threadIdx.x; i < n; i += THREADS) {
         P[i] = pin[B.prof_off + i];
     }
@@ -139,106 +173,145 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             W[k] = w[d < 0 ? d + nmax : d];
         }
     }
-    __syncthreads();
-    // thread = (row group g of 4 consecutive rows, slice q of the m range);
-    // the four rows read W at consecutive places, so stepping m slides a
-    // register window by one: 2 shared loads per 4 multiply-adds
-    float* partial = W + 2 * n;          // [Q][n]
-    const int G = n >> 2;
-    const int Q = G >= THREADS ? 1 : THREADS / G;
-    if (sum_here) {
-        const int q = threadIdx.x / (THREADS / Q);
-        const int span = n / Q;
-        const int m0 = q * span;
-        for (int g = threadIdx.x % (THREADS / Q); g < G; g += THREADS / Q) {
-            const int x = 4 * g;
-            int bidx = x - m0 + n - 1;   // W index of (row x, m0)
-            float w0 = W[bidx], w1 = W[bidx + 1], w2 = W[bidx + 2],
-                  w3 = W[bidx + 3];
-            float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
-            for (int m = m0; m < m0 + span; m++) {
-                const float pm = P[m];
-                a0 = fmaf(pm, w0, a0);
-                a1 = fmaf(pm, w1, a1);
-                a2 = fmaf(pm, w2, a2);
-                a3 = fmaf(pm, w3, a3);
-                w3 = w2;
-                w2 = w1;
-                w1 = w0;
-                bidx--;
-                w0 = W[bidx > 0 ? bidx : 0];
-            }
-            float* pr = partial + size_t(q) * n + x;
-            pr[0] = a0;
-            pr[1] = a1;
-            pr[2] = a2;
-            pr[3] = a3;
-        }
+    // loads for the later phases, issued now
+    const float* ws = tabs + B.tab_off + TAB_WS * n;
+    const int x0 = threadIdx.x;
+    const float ws0 = x0 < n ? ws[x0] : 0.f;
+    const RowStencil* rf = st + B.st_off + ST_RF * n;
+    RowStencil sb0 = {};
+    if (B.chain == 0 && x0 < n) {
+        sb0 = rf[x0];
     }
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // charge integral (src/PS/PhaseSpace.cpp:200-239), compensated:
+    // per-warp sums now, the block total after the barrier that ends the
+    // wake sum
+    {
+        FF a = x0 < n ? ff_prod(P[x0], ws0) : FF{0.f, 0.f};
+        for (int i = x0 + THREADS; i < n; i += THREADS) {
+            a = ff_add(a, ff_prod(P[i], ws[i]));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const FF t{__shfl_down_sync(0xffffffffu, a.hi, o),
+                       __shfl_down_sync(0xffffffffu, a.lo, o)};
+            a = ff_add(a, t);
+        }
+        if (lane == 0) {
+            red[warp] = make_float2(a.hi, a.lo);
+        }
+    }
+    // Toeplitz sum wake[x] = sum_m W[x - m + n - 1] P[m].  Thread = (group
+    // g of 8 consecutive rows, slice q of the m range).  The 8 rows read W
+    // at consecutive places, so stepping m slides a register window by one:
+    // 2 shared loads per 8 multiply-adds.  Lane g walks its slice from
+    // offset 7g (mod span) and wraps once, which puts the lanes of a warp
+    // on different banks for both loads (n is a power of two, 64..2048).
+    float* partial = W + 2 * n;          // [Q][n], Q n = 8 THREADS
+    const int G = n >> 3;                // <= THREADS
+    const int Q = THREADS / G;
+    if (sum_here) {
+        const int q = threadIdx.x / G;
+        const int g = threadIdx.x % G;
+        const int span = n / Q;
+        const int m0 = q * span;
+        const int x = 8 * g;
+        const int r = (7 * g) & (span - 1);
+        float acc[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            acc[j] = 0.f;
+        }
+#pragma unroll 1
+        for (int part = 0; part < 2; part++) {
+            const int mb = part == 0 ? m0 + r : m0;
+            const int me = part == 0 ? m0 + span : m0 + r;
+            int bidx = x - mb + n - 1;   // W index of (row x, mb), >= 0
+            float w[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                w[j] = W[bidx + j];
+            }
+#pragma unroll 4
+            for (int m = mb; m < me; m++) {
+                const float pm = P[m];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    acc[j] = fmaf(pm, w[j], acc[j]);
+                }
+#pragma unroll
+                for (int j = 7; j > 0; j--) {
+                    w[j] = w[j - 1];
+                }
+                bidx--;
+                w[0] = W[bidx > 0 ? bidx : 0];
+            }
+        }
+        float* pr = partial + size_t(q) * n + x;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            pr[j] = acc[j];
+        }
+    }
+    __syncthreads();   // partial sums, per-warp integrals and ticket_s
+    FF tot = FF{0.f, 0.f};
+    if (lane < (THREADS >> 5)) {
+        const float2 r = red[lane];
+        tot = FF{r.x, r.y};
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {   // same bits in every thread
+        const FF t{__shfl_xor_sync(0xffffffffu, tot.hi, o),
+                   __shfl_xor_sync(0xffffffffu, tot.lo, o)};
+        tot = ff_add(tot, t);
+    }
+    const unsigned step = static_cast<unsigned>(ticket_s / gridDim.x);
+    const bool renorm_now = B.renorm > 0 && (step % unsigned(B.renorm)) == 0;
+    float fac = 1.f;
+    if (renorm_now && B.fillset > 0) {
+        const double a = double(tot.hi) + double(tot.lo);
+        fac = static_cast<float>(double(B.fillset) / a);
+    } else if (renorm_now) {
+        fac = 0.f;
+    }
+    if (threadIdx.x == 0) {
+        filling[b] = double(tot.hi) + double(tot.lo);
+        factor[b] = fac;
+        if (B.fillset > 0 && !(tot.hi > 0.f)) {
+            atomicCAS(status, 0, VFPS_ERR_NUMERIC);
+        }
+    }
+    // wake potential of every row and, for chain 0, both y-kick stencils
+    // of the row for this step, the renormalisation factor folded into the
+    // first (both kicks are linear)
+    const bool chain0 = B.chain == 0;
     for (int x = threadIdx.x; x < n; x += THREADS) {
         float v = 0.f;
         if (sum_here) {
-            float s = 0.f;
-            for (int q = 0; q < Q; q++) {
-                s += partial[size_t(q) * n + x];
+            float sum = 0.f;
+            for (int k = 0; k < Q; k++) {
+                sum += partial[size_t(k) * n + x];
             }
-            v = __fmul_rn(B.wakescale, s);
+            v = __fmul_rn(B.wakescale, sum);
             wake[B.prof_off + x] = v;
         } else if (has_wake) {
             v = wake[B.prof_off + x];
         } else {
             wake[B.prof_off + x] = 0.f;
         }
-        partial[x] = v;    // this thread read partial[.][x] last
-    }
-    // charge integral (src/PS/PhaseSpace.cpp:200-239) in FP64
-    const float* ws = tabs + B.tab_off + TAB_WS * n;
-    double a = 0;
-    for (int i = threadIdx.x; i < n; i += THREADS) {
-        a += double(P[i]) * double(ws[i]);
-    }
-    a = block_sum(a, red);
-    if (threadIdx.x == 0) {
-        filling[b] = a;
-        const bool renorm_now = B.renorm > 0
-                                && (step % unsigned(B.renorm)) == 0;
-        float f = 1.f;
-        if (renorm_now) {
-            f = B.fillset > 0 ? static_cast<float>(double(B.fillset) / a) : 0.f;
+        if (!chain0) {
+            continue;
         }
-        factor[b] = f;
-        fac_s = f;
-        if (B.fillset > 0 && !(a > 0)) {
-            atomicCAS(status, 0, VFPS_ERR_NUMERIC);
-        }
-        // the last CTA of the step advances the step counter
-        __threadfence();
-        const unsigned ticket = atomicAdd(counters + 1, 1u);
-        if (ticket == gridDim.x - 1) {
-            counters[1] = 0;
-            counters[0] = step + 1;
-            __threadfence();
-        }
-    }
-    if (B.chain != 0) {
-        return;
-    }
-    // chain 0: both y-kick stencils of every row for this step, the
-    // renormalisation factor folded into the first (both kicks are linear)
-    __syncthreads();
-    const float fac = fac_s;
-    const RowStencil* rf = st + B.st_off + ST_RF * n;
-    for (int x = threadIdx.x; x < n; x += THREADS) {
         RowStencil sa;
         if (has_wake) {
-            sa = make_stencil(partial[x], B.n, int(B.it));
+            sa = make_stencil(v, B.n, int(B.it));
         } else {
             sa.shift0 = 0;
             sa.w[0] = 1.f;
             sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
         }
-        const RowStencil sb = rf[x];
+        const RowStencil sb = x == x0 ? sb0 : rf[x];
         RowInfo ri;
         ri.s = sa.shift0 + sb.shift0;
         ri.sb = sb.shift0;
@@ -981,6 +1054,8 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         mbar_fence_init();
     }
     fence_proxy_async();
+    // this step's stencils and the previous step's density are complete
+    pdl_wait();
     __syncthreads();
 
     // each CTA walks a contiguous chunk of the tile list: tiles of a bunch

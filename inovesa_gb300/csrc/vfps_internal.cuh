@@ -408,6 +408,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return done != 0;
 }
 
+// Programmatic dependent launch: let the next kernel of the stream (one
+// launched with programmatic stream serialisation) start its independent
+// prologue, and wait until the previous kernel has completed and its
+// memory is visible before reading or writing anything it touches.
+__device__ __forceinline__ void pdl_trigger()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+__device__ __forceinline__ void pdl_wait()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 __device__ __forceinline__ uint64_t global_ns()
 {
     uint64_t t;
