@@ -156,8 +156,9 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             VFPS_CUDA(cudaEventRecord(ev[i], st));
         }
     };
-    // P[n], W[2n], partial sums [Q][n] with Q n = 8 THREADS
-    const size_t wsm = (3 * size_t(b->max_n) + 8 * THREADS) * sizeof(float);
+    // P[n], padded W[2n + n/4], partial sums [Q][n] with Q n = 8 THREADS
+    const size_t wsm = (3 * size_t(b->max_n) + b->max_n / 4 + 8 * THREADS)
+                       * sizeof(float);
     mark(0);
     const bool tc = b->wake_tc && b->tc_groups > 0;
     if (tc) {

@@ -155,7 +155,9 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     const uint32_t b = blockIdx.x;
     const BDev B = bd[b];
     const int n = int(B.n);
-    float* W = P + n;   // W[k] = w[(k - (n-1)) mod nmax], k < 2n - 1
+    // W[k + k/8] = w[(k - (n-1)) mod nmax] for k < 2n - 1: one pad entry
+    // per 8 puts the 32 lanes of the wake sum (rows 8 apart) on 32 banks
+    float* W = P + n;
     if (threadIdx.x == 0) {
         ticket_s = atomicAdd(tickets, 1ull);
     }
@@ -170,7 +172,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         const float* w = wt + B.wt_off;
         for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
             const int d = k - (n - 1);   // |d| < n <= nmax / 2
-            W[k] = w[d < 0 ? d + nmax : d];
+            W[k + (k >> 3)] = w[d < 0 ? d + nmax : d];
         }
     }
     // loads for the later phases, issued now
@@ -202,14 +204,14 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             red[warp] = make_float2(a.hi, a.lo);
         }
     }
-    // Toeplitz sum wake[x] = sum_m W[x - m + n - 1] P[m].  Thread = (group
-    // g of 8 consecutive rows, slice q of the m range).  The 8 rows read W
-    // at consecutive places, so stepping m slides a register window by one:
-    // 2 shared loads per 8 multiply-adds.  Lane g walks its slice from
-    // offset 7g (mod span) and wraps once, which puts the lanes of a warp
-    // on different banks for both loads (n is a power of two, 64..2048).
-    float* partial = W + 2 * n;          // [Q][n], Q n = 8 THREADS
-    const int G = n >> 3;                // <= THREADS
+    // Toeplitz sum wake[x] = sum_m w[x - m] P[m] (W index x - m + n - 1).
+    // Thread = (group g of 8 consecutive rows, slice q of the m range); the
+    // 8 rows read W at consecutive places, so stepping m slides a register
+    // window by one: 2 shared loads (P broadcast, W padded) per 8
+    // multiply-adds, the same trip count in every lane (n is a power of
+    // two, 64..2048).
+    float* partial = W + 2 * n + (n >> 2);   // [Q][n], Q n = 8 THREADS
+    const int G = n >> 3;                    // <= THREADS
     const int Q = THREADS / G;
     if (sum_here) {
         const int q = threadIdx.x / G;
@@ -217,36 +219,28 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         const int span = n / Q;
         const int m0 = q * span;
         const int x = 8 * g;
-        const int r = (7 * g) & (span - 1);
-        float acc[8];
+        int bidx = x - m0 + n - 1;   // W index of (row x, m0)
+        float w[8], acc[8];
 #pragma unroll
         for (int j = 0; j < 8; j++) {
+            const int k = bidx + j;
+            w[j] = W[k + (k >> 3)];
             acc[j] = 0.f;
         }
-#pragma unroll 1
-        for (int part = 0; part < 2; part++) {
-            const int mb = part == 0 ? m0 + r : m0;
-            const int me = part == 0 ? m0 + span : m0 + r;
-            int bidx = x - mb + n - 1;   // W index of (row x, mb), >= 0
-            float w[8];
+#pragma unroll 4
+        for (int m = m0; m < m0 + span; m++) {
+            const float pm = P[m];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
-                w[j] = W[bidx + j];
+                acc[j] = fmaf(pm, w[j], acc[j]);
             }
-#pragma unroll 4
-            for (int m = mb; m < me; m++) {
-                const float pm = P[m];
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    acc[j] = fmaf(pm, w[j], acc[j]);
-                }
-#pragma unroll
-                for (int j = 7; j > 0; j--) {
-                    w[j] = w[j - 1];
-                }
-                bidx--;
-                w[0] = W[bidx > 0 ? bidx : 0];
+            for (int j = 7; j > 0; j--) {
+                w[j] = w[j - 1];
             }
+            bidx--;
+            const int k = bidx > 0 ? bidx : 0;
+            w[0] = W[k + (k >> 3)];
         }
         float* pr = partial + size_t(q) * n + x;
 #pragma unroll
