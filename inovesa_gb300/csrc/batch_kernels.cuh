@@ -31,7 +31,7 @@ constexpr int TPAD = 4;        // zero floats on each side of a t3 row
 constexpr int APAD = 32;       // zero floats left of a staged row (chain 0)
 constexpr uint64_t WAIT_NS = 1000000000ull;  // bounded TMA waits (1 s)
 
-struct BDev {
+struct __align__(16) BDev {     // 96 bytes: vector loads of its fields
     uint32_t n, it, chain, flags;  // flags: F_*
     uint32_t dens_off, prof_off, tab_off, st_off;
     uint32_t fp_off, wt_off, nmax, rot_h;
@@ -41,9 +41,18 @@ struct BDev {
     float zbq, zbp, cs, sn;
 };
 
-struct Tile {
+struct __align__(16) Tile {
     uint32_t bunch, x0, rows, pad;
 };
+static_assert(sizeof(BDev) == 96 && sizeof(Tile) == 16,
+              "host and device share these layouts");
+
+// log2 of seg = n / 8 lanes per row (n a power of two): the lane splits
+// below are shifts and masks instead of divisions by a runtime value
+__device__ __forceinline__ int lg_seg(int n)
+{
+    return __ffs(n) - 4;
+}
 
 // one kick stencil: tap j reads cell i + shift0 + j with weight w[j]
 // (dropped taps have weight 0)
@@ -370,9 +379,10 @@ __device__ __forceinline__ void fp_and_store(
     float* part)
 {
     const int seg = n >> 3;               // threads per row
-    const int rp = THREADS / seg;         // rows in parallel
-    const int l = threadIdx.x % seg;
-    const int rl = threadIdx.x / seg;
+    const int lg = lg_seg(n);
+    const int rp = THREADS >> lg;         // rows in parallel
+    const int l = threadIdx.x & (seg - 1);
+    const int rl = threadIdx.x >> lg;
     const int y0 = 8 * l;
     const int stride = n + 2 * TPAD;
     {
@@ -623,9 +633,10 @@ k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         // are read as five aligned float4 and picked at the row alignment.
         {
             const int seg = n >> 3;
-            const int rp = THREADS / seg;
-            const int l = threadIdx.x % seg;
-            const int rl = threadIdx.x / seg;
+            const int lg = lg_seg(n);
+            const int rp = THREADS >> lg;
+            const int l = threadIdx.x & (seg - 1);
+            const int rl = threadIdx.x >> lg;
             const int y0 = 8 * l;
             for (int r = rl; r < nr; r += rp) {
                 const RowInfo ri = S[r];
@@ -1097,7 +1108,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             }
             // lanes of one row: a segment of seg lanes of this warp
             const unsigned rmask = seg == 32 ? 0xffffffffu
-                : (((1u << seg) - 1u) << ((lane / seg) * seg));
+                : (((1u << seg) - 1u) << (lane & ~(seg - 1)));
             const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int i = rl; i < m; i += rp) {
                 const int x = lo_c + i;
