@@ -359,6 +359,22 @@ VFPS_API int vfps_batch_upload(vfps_batch* batch, const float* density);
 VFPS_API int vfps_batch_get_profiles(vfps_batch* batch, float* profiles);
 VFPS_API int vfps_batch_get_filling(vfps_batch* batch, double* filling);
 VFPS_API int vfps_batch_get_wake(vfps_batch* batch, float* wake);
+/* Replace the density of every chain-0 bunch with the stationary state of
+ * its solver step below the instability threshold, and refresh profiles
+ * and filling (as vfps_batch_upload does).  The reference names this
+ * start only as an ignored option (HaissinskiIterations,
+ * src/IO/ProgramOptions.cpp:270); here it is the Haissinski potential
+ * well of the wake and RF kicks, written as a function of the invariant
+ * of the discrete step (kick, then drift):
+ *   density(x, y) ~ exp(-(Phi(x) + G(y) + F(x) d(y) / 2) / T),
+ * F = -(rf + wake) the y-kick of row x, Phi its integral, d the drift
+ * offset of column y, G its integral, T = slip0 / (dq dp).  The wake
+ * depends on the profile: `iterations` fixed-point passes, each mixing
+ * `mix` (0 < mix <= 1) of the new profile into the old.  change[nb]
+ * (optional) receives the last relative L1 change of each profile
+ * (0 for bunches without a wake; chain-1 bunches are left as they are). */
+VFPS_API int vfps_batch_potential_well(vfps_batch* batch, uint32_t iterations,
+                                       float mix, float* change);
 /* kernel launches per solver step (for launch accounting) */
 VFPS_API int vfps_batch_info(const vfps_batch* batch, uint32_t* launches,
                              uint32_t* tile_rows);

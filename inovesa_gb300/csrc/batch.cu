@@ -53,6 +53,8 @@ struct vfps_batch {
     DevBuf<Tile> tiles[TL_COUNT];
     DevBuf<float> tabs, fp5, wt, dwt;
     DevBuf<RowStencil> st;
+    DevBuf<PwDev> pw;          // potential-well state: per bunch
+    DevBuf<float> pwtab;       // raw RF and drift offsets of chain 0
     DevBuf<uint32_t> row_bunch;
     DevBuf<float> dens[2], prof[2];
     DevBuf<float> wake, factor;
@@ -632,7 +634,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         b->nb = nb;
         b->desc.assign(desc, desc + nb);
         b->hb.resize(nb);
-        std::vector<float> tabs, fp5, wt, gauss, dwt;
+        std::vector<float> tabs, fp5, wt, gauss, dwt, pwtab;
+        std::vector<PwDev> pws;
         std::map<std::string, uint32_t> dw_seen;
         std::vector<RowStencil> sts;
         std::vector<uint32_t> row_bunch, goff;
@@ -682,7 +685,13 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             tabs.insert(tabs.end(), ay.v.begin(), ay.v.end());
             // RF (per row) and drift (per column) stencils
             std::vector<RowStencil> rf(n), dr(n);
+            PwDev pwd{};
             if (d.chain == 0) {
+                // their raw offsets for the potential-well state
+                pwd.off = static_cast<uint32_t>(pwtab.size());
+                pwd.T = static_cast<float>(d.slip[0])
+                        / (ax.delta * ay.delta);
+                pwtab.resize(pwtab.size() + 2 * size_t(n), 0.f);
                 const float bl2phase = static_cast<float>(d.rf_bl2phase);
                 for (uint32_t x = 0; x < n; x++) {
                     float o;
@@ -701,6 +710,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                             / ay.delta / ay.scale;
                     }
                     rf[x] = host_stencil(o, n, d.it);
+                    pwtab[pwd.off + x] = o;
                 }
                 // src/SM/DriftMap.cpp:21-30
                 const float e0 = float(d.e0);
@@ -713,6 +723,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                     }
                     o /= ax.delta;
                     dr[y] = host_stencil(o, n, d.it);
+                    pwtab[pwd.off + n + y] = o;
                     lo = std::min(lo, dr[y].shift0);
                     hi = std::max(hi, dr[y].shift0 + 3);
                 }
@@ -747,6 +758,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             }
             sts.insert(sts.end(), rf.begin(), rf.end());
             sts.insert(sts.end(), dr.begin(), dr.end());
+            pws.push_back(pwd);
             if (d.chain == 0) {
                 // drift stencils as planes for 16-byte loads: w[j][y] for
                 // j < 4, then shift0[y] (int bits), then the Fokker-Planck
@@ -851,6 +863,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         put(b->st, sts);
         put(b->fp5, fp5);
         put(b->dwt, dwt);
+        put(b->pw, pws);
+        put(b->pwtab, pwtab);
         b->wt.alloc(std::max<size_t>(wt.size(), 1));
         for (uint32_t k = 0; k < nimp; k++) {
             if (wt_off[k] != 0xffffffffu) {
@@ -1175,6 +1189,36 @@ extern "C" int vfps_batch_get_wake(vfps_batch* b, float* wake)
     return bguard(b->ctx, [&] {
         copy_packed(b, wake, true, true, b->wake.p);
         VFPS_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    });
+}
+
+extern "C" int vfps_batch_potential_well(vfps_batch* b, uint32_t iterations,
+                                         float mix, float* change)
+{
+    if (!b || iterations > 100000 || !(mix > 0.f) || mix > 1.f) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    return bguard(b->ctx, [&] {
+        cudaStream_t st = b->ctx->stream;
+        const size_t smem = pw_smem(b->max_n).total * sizeof(float);
+        VFPS_CUDA(cudaFuncSetAttribute(
+            k_potential_well, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            static_cast<int>(smem)));
+        DevBuf<float> ch(b->nb);
+        VFPS_CUDA(cudaMemsetAsync(ch.p, 0, ch.bytes(), st));
+        k_potential_well<<<b->nb, THREADS, smem, st>>>(
+            b->bd.p, b->pw.p, b->pwtab.p, b->tabs.p, b->wt.p,
+            b->dens[b->cur].p, ch.p, b->ctx->d_status,
+            static_cast<int>(iterations), mix);
+        VFPS_LAUNCHED();
+        // profiles and filling of the new state (as after an upload)
+        project_all(b, b->cur);
+        integrate_all(b, b->cur, 0);
+        if (change) {
+            VFPS_CUDA(cudaMemcpyAsync(change, ch.p, ch.bytes(),
+                                      cudaMemcpyDeviceToHost, st));
+        }
+        VFPS_CUDA(cudaStreamSynchronize(st));
     });
 }
 

@@ -142,6 +142,66 @@ __device__ __forceinline__ FF ff_add(FF a, FF b)
     return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
 }
 
+// Toeplitz sum wake[x] = sum_m w[x - m] P[m] of a CTA of THREADS threads,
+// from W[k + k/8] = w[k - (n-1)] (one pad entry per 8 puts the lanes below
+// on 32 banks).  Thread = (group g of 8 consecutive rows, slice q of the m
+// range); the 8 rows read W at consecutive places, so stepping m slides a
+// register window by one: 2 shared loads (P broadcast, W) per 8
+// multiply-adds, the same trip count in every lane.  Writes the partial
+// sums partial[q][x] (Q = THREADS / (n/8) slices; n a power of two,
+// 64..2048); the caller sums them after a barrier.
+__device__ __forceinline__ void toeplitz_partials(const float* P,
+                                                  const float* W,
+                                                  float* partial, int n)
+{
+    const int G = n >> 3;                    // <= THREADS
+    const int Q = THREADS / G;
+    const int q = threadIdx.x / G;
+    const int g = threadIdx.x % G;
+    const int span = n / Q;
+    const int m0 = q * span;
+    const int x = 8 * g;
+    int bidx = x - m0 + n - 1;   // W index of (row x, m0)
+    float w[8], acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int k = bidx + j;
+        w[j] = W[k + (k >> 3)];
+        acc[j] = 0.f;
+    }
+#pragma unroll 4
+    for (int m = m0; m < m0 + span; m++) {
+        const float pm = P[m];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            acc[j] = fmaf(pm, w[j], acc[j]);
+        }
+#pragma unroll
+        for (int j = 7; j > 0; j--) {
+            w[j] = w[j - 1];
+        }
+        bidx--;
+        const int k = bidx > 0 ? bidx : 0;
+        w[0] = W[k + (k >> 3)];
+    }
+    float* pr = partial + size_t(q) * n + x;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        pr[j] = acc[j];
+    }
+}
+
+// W[k + k/8] = w[(k - (n-1)) mod nmax] for k < 2n - 1 (the layout that
+// toeplitz_partials reads; |k - (n-1)| < n <= nmax / 2)
+__device__ __forceinline__ void load_toeplitz(const float* __restrict__ w,
+                                              int nmax, int n, float* W)
+{
+    for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
+        const int d = k - (n - 1);
+        W[k + (k >> 3)] = w[d < 0 ? d + nmax : d];
+    }
+}
+
 // One CTA per bunch: wake potential of the previous step's profile, charge
 // integral, renormalisation factor and, for chain 0, both y-kick stencils
 // of every row.  The step number comes from a 64-bit ticket that every CTA
@@ -177,12 +237,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     // wake_ready: the tensor-core kernel has written this step's wake
     const bool sum_here = has_wake && !wake_ready;
     if (sum_here) {
-        const int nmax = int(B.nmax);
-        const float* w = wt + B.wt_off;
-        for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
-            const int d = k - (n - 1);   // |d| < n <= nmax / 2
-            W[k + (k >> 3)] = w[d < 0 ? d + nmax : d];
-        }
+        load_toeplitz(wt + B.wt_off, int(B.nmax), n, W);
     }
     // loads for the later phases, issued now
     const float* ws = tabs + B.tab_off + TAB_WS * n;
@@ -213,49 +268,10 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             red[warp] = make_float2(a.hi, a.lo);
         }
     }
-    // Toeplitz sum wake[x] = sum_m w[x - m] P[m] (W index x - m + n - 1).
-    // Thread = (group g of 8 consecutive rows, slice q of the m range); the
-    // 8 rows read W at consecutive places, so stepping m slides a register
-    // window by one: 2 shared loads (P broadcast, W padded) per 8
-    // multiply-adds, the same trip count in every lane (n is a power of
-    // two, 64..2048).
     float* partial = W + 2 * n + (n >> 2);   // [Q][n], Q n = 8 THREADS
-    const int G = n >> 3;                    // <= THREADS
-    const int Q = THREADS / G;
+    const int Q = THREADS / (n >> 3);
     if (sum_here) {
-        const int q = threadIdx.x / G;
-        const int g = threadIdx.x % G;
-        const int span = n / Q;
-        const int m0 = q * span;
-        const int x = 8 * g;
-        int bidx = x - m0 + n - 1;   // W index of (row x, m0)
-        float w[8], acc[8];
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int k = bidx + j;
-            w[j] = W[k + (k >> 3)];
-            acc[j] = 0.f;
-        }
-#pragma unroll 4
-        for (int m = m0; m < m0 + span; m++) {
-            const float pm = P[m];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                acc[j] = fmaf(pm, w[j], acc[j]);
-            }
-#pragma unroll
-            for (int j = 7; j > 0; j--) {
-                w[j] = w[j - 1];
-            }
-            bidx--;
-            const int k = bidx > 0 ? bidx : 0;
-            w[0] = W[k + (k >> 3)];
-        }
-        float* pr = partial + size_t(q) * n + x;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            pr[j] = acc[j];
-        }
+        toeplitz_partials(P, W, partial, n);
     }
     __syncthreads();   // partial sums, per-warp integrals and ticket_s
     FF tot = FF{0.f, 0.f};
@@ -325,6 +341,278 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         }
         ri.pad[0] = ri.pad[1] = 0;
         rinfo[B.prof_off + x] = ri;
+    }
+}
+
+// ------------------------------------------------------ potential well
+// Per chain-0 bunch: offsets of the RF kick (per row) and of the drift (per
+// column) in pwtab, and the energy scale T of the state below
+struct PwDev {
+    uint32_t off;  // rf offsets [n], then drift offsets [n]
+    float T;       // slip0 / (dq dp)
+    float pad[2];
+};
+
+// float offsets of the regions of k_potential_well's dynamic shared memory
+// for a mesh of n rows (every region grows with n, so the layout of the
+// largest mesh of a batch covers the others)
+struct PwSmem {
+    size_t P, W, partial, F, Phi, G, D, RF, WS, M, S, total;
+};
+
+__host__ __device__ inline PwSmem pw_smem(size_t n)
+{
+    PwSmem L;
+    L.P = 0;                          // profile [n]
+    L.W = L.P + n;                    // Toeplitz table [2n + n/4]
+    L.partial = L.W + 2 * n + n / 4;  // partial sums [8 THREADS]
+    L.F = L.partial + 8 * THREADS;    // row kicks [n]
+    L.Phi = L.F + n;                  // their integral [n]
+    L.G = L.Phi + n;                  // integral of the drift offsets [n]
+    L.D = L.G + n;                    // drift offsets [n]
+    L.RF = L.D + n;                   // RF offsets [n]
+    L.WS = L.RF + n;                  // Simpson weights [n]
+    L.M = L.WS + n;                   // row maxima [n]
+    L.S = L.M + n;                    // row sums [n]
+    L.total = L.S + n;
+    return L;
+}
+
+// block-wide trapezoid integral: out[0] = 0, out[i] = out[i-1] +
+// (f[i-1] + f[i]) / 2; each thread sums a run of consecutive entries
+__device__ void block_trapezoid(const float* f, float* out, int n,
+                                float* scratch32)
+{
+    const int per = (n + THREADS - 1) / THREADS;
+    const int i0 = threadIdx.x * per;
+    const int i1 = min(n, i0 + per);
+    float run = 0.f;
+    for (int i = max(i0, 1); i < i1; i++) {
+        run += 0.5f * (f[i - 1] + f[i]);
+    }
+    // exclusive scan of the per-thread sums: within warps, then warps
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const float v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) {
+            inc += v;
+        }
+    }
+    if (lane == 31) {
+        scratch32[warp] = inc;
+    }
+    __syncthreads();
+    float base = 0.f;
+    for (int w = 0; w < warp; w++) {
+        base += scratch32[w];
+    }
+    float acc = base + inc - run;
+    for (int i = i0; i < i1; i++) {
+        if (i > 0) {
+            acc += 0.5f * (f[i - 1] + f[i]);
+        }
+        out[i] = acc;
+    }
+    __syncthreads();
+}
+
+__device__ float block_max(float v, float* scratch32)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+        scratch32[warp] = v;
+    }
+    __syncthreads();
+    float m = scratch32[0];
+    for (int w = 1; w < (THREADS >> 5); w++) {
+        m = fmaxf(m, scratch32[w]);
+    }
+    return m;
+}
+
+__device__ float block_sum_f(float v, float* scratch32)
+{
+    v = warp_sum_f(v);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) {
+        scratch32[warp] = v;
+    }
+    __syncthreads();
+    float t = 0.f;
+    for (int w = 0; w < (THREADS >> 5); w++) {
+        t += scratch32[w];
+    }
+    return t;
+}
+
+// The stationary state of the chain-0 step (y-kicks of the wake and the
+// RF, drift, Fokker-Planck) below the instability threshold: a function of
+// the step's invariant, exp(-E / T) with
+//   E(x, y) = Phi(x) + G(y) + F(x) d(y) / 2,
+// F = -(rf + wake) the y-kick of row x (cells per step), Phi its integral
+// over x, d the drift offset of column y, G its integral over y, and T =
+// slip0 / (dq dp) the scale at which the Fokker-Planck term holds the
+// energy spread at one unit.  Phi + G is the Haissinski potential well
+// (the continuous-time invariant); the cross term is the first correction
+// of the split step (kick, then drift) to it.  The wake depends on the
+// profile, so the profile iterates to a fixed point (mixing `mix` of each
+// new profile into the old one).  One CTA per bunch; bunches of chain 1
+// are left as they are.  Writes the density normalised to the bunch's
+// filling and the last relative L1 change of the profile.
+__global__ void __launch_bounds__(THREADS)
+k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
+                 const float* __restrict__ pwtab,
+                 const float* __restrict__ tabs,
+                 const float* __restrict__ wt, float* __restrict__ dens,
+                 float* __restrict__ change, int* __restrict__ status,
+                 int iters, float mix)
+{
+    const BDev B = bd[blockIdx.x];
+    if (B.chain != 0) {
+        return;
+    }
+    extern __shared__ float4 pwsm4[];
+    __shared__ float scratch[32];
+    const int n = int(B.n);
+    const PwSmem L = pw_smem(size_t(n));
+    uint32_t dyn_bytes;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn_bytes));
+    if (L.total * sizeof(float) > dyn_bytes) {   // the launch's layout
+        if (threadIdx.x == 0) {
+            atomicCAS(status, 0, VFPS_ERR_INVALID_ARGUMENT);
+        }
+        return;
+    }
+    float* base = reinterpret_cast<float*>(pwsm4);
+    float* P = base + L.P;
+    float* W = base + L.W;
+    float* partial = base + L.partial;
+    float* F = base + L.F;
+    float* Phi = base + L.Phi;
+    float* G = base + L.G;
+    float* D = base + L.D;
+    float* RF = base + L.RF;
+    float* WS = base + L.WS;
+    float* M = base + L.M;
+    float* S = base + L.S;
+    const PwDev Z = pw[blockIdx.x];
+    const float* ws = tabs + B.tab_off + TAB_WS * n;
+    for (int i = threadIdx.x; i < n; i += THREADS) {
+        RF[i] = pwtab[Z.off + i];
+        D[i] = pwtab[Z.off + n + i];
+        WS[i] = ws[i];
+        P[i] = 0.f;
+    }
+    const bool has_wake = B.flags & F_WAKE;
+    if (has_wake) {
+        load_toeplitz(wt + B.wt_off, int(B.nmax), n, W);
+    }
+    __syncthreads();
+    block_trapezoid(D, G, n, scratch);
+    {
+        float gmin = 3.4e38f;
+        for (int i = threadIdx.x; i < n; i += THREADS) {
+            gmin = fminf(gmin, G[i]);
+        }
+        gmin = -block_max(-gmin, scratch);
+        for (int i = threadIdx.x; i < n; i += THREADS) {
+            G[i] -= gmin;
+        }
+        __syncthreads();
+    }
+    const float fill = B.fillset > 0 ? B.fillset : 1.f;
+    const float invT = 1.f / Z.T;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int Q = THREADS / (n >> 3);
+    float delta = 0.f;
+    const int last = has_wake ? iters : 0;   // without a wake: one pass
+    for (int it = 0; it <= last; it++) {
+        // row kicks of the current profile (the first pass: RF only)
+        if (has_wake && it > 0) {
+            toeplitz_partials(P, W, partial, n);
+        }
+        __syncthreads();
+        for (int x = threadIdx.x; x < n; x += THREADS) {
+            float wake = 0.f;
+            if (has_wake && it > 0) {
+                float sum = 0.f;
+                for (int k = 0; k < Q; k++) {
+                    sum += partial[size_t(k) * n + x];
+                }
+                wake = __fmul_rn(B.wakescale, sum);
+            }
+            F[x] = -(RF[x] + wake);
+        }
+        __syncthreads();
+        block_trapezoid(F, Phi, n, scratch);
+        // per row: maximum of the exponent and the Simpson sum over y
+        for (int x = warp; x < n; x += THREADS >> 5) {
+            const float phi = Phi[x], hf = 0.5f * F[x];
+            float m = -3.4e38f;
+            for (int y = lane; y < n; y += 32) {
+                m = fmaxf(m, -(phi + G[y] + hf * D[y]) * invT);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            }
+            float sum = 0.f;
+            for (int y = lane; y < n; y += 32) {
+                sum += WS[y] * expf(-(phi + G[y] + hf * D[y]) * invT - m);
+            }
+            sum = warp_sum_f(sum);
+            if (lane == 0) {
+                M[x] = m;
+                S[x] = sum;
+            }
+        }
+        __syncthreads();
+        float mloc = -3.4e38f;
+        for (int x = threadIdx.x; x < n; x += THREADS) {
+            mloc = fmaxf(mloc, M[x]);
+        }
+        const float mx = block_max(mloc, scratch);
+        float mass = 0.f;
+        for (int x = threadIdx.x; x < n; x += THREADS) {
+            mass += WS[x] * S[x] * expf(M[x] - mx);
+        }
+        mass = block_sum_f(mass, scratch);
+        const float scale = fill / mass;
+        if (it == last) {
+            // the state: exp(-E / T) scaled to the filling
+            float* out = dens + B.dens_off;
+            for (int x = warp; x < n; x += THREADS >> 5) {
+                const float phi = Phi[x], hf = 0.5f * F[x];
+                for (int y = lane; y < n; y += 32) {
+                    out[size_t(x) * n + y] =
+                        scale * expf(-(phi + G[y] + hf * D[y]) * invT - mx);
+                }
+            }
+            break;
+        }
+        // new profile, its change against the current one, mixing
+        float dsum = 0.f, psum = 0.f;
+        for (int x = threadIdx.x; x < n; x += THREADS) {
+            const float r = scale * S[x] * expf(M[x] - mx);
+            dsum += fabsf(r - P[x]);
+            psum += fabsf(P[x]);
+            P[x] = it == 0 ? r : fmaf(mix, r - P[x], P[x]);
+        }
+        dsum = block_sum_f(dsum, scratch);
+        psum = block_sum_f(psum, scratch);
+        delta = psum > 0.f ? dsum / psum : 1.f;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        change[blockIdx.x] = delta;
     }
 }
 

@@ -707,6 +707,16 @@ class BunchBatch(_Handle):
         _, off = self.layout(b)
         return self.profiles()[off:off + int(self.descs[b].n)]
 
+    def potential_well(self, iterations=200, mix=0.5):
+        """Replace every chain-0 density by the stationary state of its
+        step below threshold (the Haissinski potential well written in the
+        invariant of the discrete kick-drift step); returns the last
+        relative change of each profile in the fixed-point iteration."""
+        out = np.zeros(len(self.descs), np.float32)
+        self._check(lib().vfps_batch_potential_well(
+            self._h, int(iterations), float(mix), _fptr(out)))
+        return out
+
     def wake(self):
         out = np.empty(self.rows, np.float32)
         self._check(lib().vfps_batch_get_wake(self._h, _fptr(out)))

@@ -1,6 +1,10 @@
-"""Learned warm start: a small network that proposes the equilibrium density
-of a bunch from its normalised current S, gap ratio g/R and damping time
-(in synchrotron periods), trained on equilibria this solver produced.
+"""Learned warm start: the equilibrium density of a bunch proposed from
+its normalised current S, gap ratio g/R and damping time (in synchrotron
+periods).  The proposal is the potential-well state of the bunch's step
+(vfps_batch_potential_well: the Haissinski solution written in the
+invariant of the discrete kick-drift step, computed on the device) plus a
+correction that a small network predicts, trained on the difference
+between equilibria this solver produced and that state.
 
 The proposal enters the solver as initial data (the reference's
 PhaseSpace data argument, inc/PS/PhaseSpace.hpp:54-61, the hook of
@@ -47,9 +51,10 @@ def run_to_equilibrium(ctx, samples, n=256, spt=1000, tol=1e-5,
     """Advance one batch of bunches period by period until the relative L1
     change of each profile over a period is below tol.
 
-    samples: (S, gap ratio, damping periods) per bunch; start: optional
-    initial densities [nb][n][n] (else the Gaussian).  Returns (final
-    densities [nb][n][n], periods needed per bunch (-1: not converged))."""
+    samples: (S, gap ratio, damping periods) per bunch; start: initial
+    densities [nb][n][n], "potential_well" (the device's potential-well
+    state) or None (the Gaussian).  Returns (final densities [nb][n][n],
+    periods needed per bunch (-1: not converged))."""
     zs, keys, descs = {}, [], []
     for S, g, td in samples:
         p = bunch_params(n, spt, S, g, td)
@@ -62,7 +67,11 @@ def run_to_equilibrium(ctx, samples, n=256, spt=1000, tol=1e-5,
     b = V.BunchBatch(ctx, descs, [zs[k] for k in keys])
     nb = len(samples)
     lay = [b.layout(i) for i in range(nb)]
-    if start is not None:
+    if isinstance(start, str):
+        if start != "potential_well":
+            raise ValueError("unknown start " + start)
+        b.potential_well()
+    elif start is not None:
         full = b.download()
         for i in range(nb):
             off = lay[i][0]
@@ -91,6 +100,16 @@ def run_to_equilibrium(ctx, samples, n=256, spt=1000, tol=1e-5,
     dens = np.stack([full[lay[i][0]:lay[i][0] + n * n].reshape(n, n)
                      for i in range(nb)])
     return dens, done
+
+
+def potential_well_states(ctx, samples, n=256, spt=1000, chunk=256):
+    """The device's potential-well state of every bunch, [nb][n][n]."""
+    out = []
+    for i in range(0, len(samples), chunk):
+        d, _ = run_to_equilibrium(ctx, samples[i:i + chunk], n=n, spt=spt,
+                                  max_periods=0, start="potential_well")
+        out.append(d)
+    return np.concatenate(out)
 
 
 def simpson_normalise(d, delta):
@@ -290,7 +309,8 @@ def equilibria(ctx, samples, n, spt, tol, max_periods, start=None,
         d, p = run_to_equilibrium(
             ctx, samples[i:i + chunk], n=n, spt=spt, tol=tol,
             max_periods=max_periods,
-            start=None if start is None else start[i:i + chunk])
+            start=start if start is None or isinstance(start, str)
+            else start[i:i + chunk])
         dens.append(d)
         done.append(p)
     return np.concatenate(dens), np.concatenate(done)
@@ -299,53 +319,73 @@ def equilibria(ctx, samples, n, spt, tol, max_periods, start=None,
 def experiment(ctx, n=256, spt=1000, ntrain=2048, ntest=128, iters=3000,
                tol=1e-5, max_periods=300, seed=7, log=None, tol_train=None,
                max_periods_train=None):
-    """Train on solver equilibria, then compare steps to equilibrium from
-    the Gaussian and from the proposal on held-out inputs.  The training
-    equilibria may be converged further than the judging tolerance
-    (tol_train): the stopping rule samples the profile once per
-    synchrotron period and leaves coherent oscillations of about a damping
-    time's worth of the tolerance, which would otherwise be learned as
-    noise."""
+    """Train the correction on solver equilibria, then compare the periods
+    to equilibrium on held-out inputs from the Gaussian, from the
+    potential-well state alone and from the proposal (potential-well state
+    plus the learned correction).  The training equilibria may be
+    converged further than the judging tolerance (tol_train): the stopping
+    rule samples the profile once per synchrotron period and leaves
+    coherent oscillations of about a damping time's worth of the
+    tolerance, which would otherwise be learned as noise."""
     rng = np.random.default_rng(seed)
     train_in = sample_inputs(rng, ntrain, True)
     test_in = sample_inputs(rng, ntest, False)
+    axes = bunch_params(n, spt, *train_in[0])["axes"]
+    dq = (axes[1] - axes[0]) / (n - 1)
+    # training targets: equilibrium (unit charge) minus potential well
     tr_d, tr_p = equilibria(ctx, train_in, n, spt, tol_train or tol,
-                            max_periods_train or max_periods)
+                            max_periods_train or max_periods,
+                            start="potential_well")
+    tr_base = potential_well_states(ctx, train_in, n, spt)
     ok = tr_p >= 0
+    resid = (simpson_normalise(tr_d[ok], dq).astype(np.float64)
+             - tr_base[ok]).reshape(int(ok.sum()), -1)
+    scale = float(resid.std()) or 1.0
     x = normalise_inputs(*np.array(train_in)[ok].T)
-    tgt = tr_d[ok].reshape(int(ok.sum()), -1)
+    tgt = (resid / scale).astype(np.float32)
     net = WarmStartNet(ctx, n * n, seed=seed)
     net.set_bias(tgt.mean(0))
     hist = train(net, x, tgt, iters=iters)
-    # held out: Gaussian start, then the proposal
+    # held out: Gaussian start, potential well, proposal
     g_d, g_p = equilibria(ctx, test_in, n, spt, tol, max_periods)
-    axes = bunch_params(n, spt, *test_in[0])["axes"]
-    dq = (axes[1] - axes[0]) / (n - 1)
-    prop = net.forward(normalise_inputs(*np.array(test_in).T))
-    prop = simpson_normalise(prop.reshape(-1, n, n), dq)
+    base = potential_well_states(ctx, test_in, n, spt)
+    _, h_p = equilibria(ctx, test_in, n, spt, tol, max_periods,
+                        start=base)
+    corr = net.forward(normalise_inputs(*np.array(test_in).T))
+    prop = simpson_normalise(base + scale * corr.reshape(-1, n, n), dq)
     w_d, w_p = equilibria(ctx, test_in, n, spt, tol, max_periods, start=prop)
-    both = (g_p > 0) & (w_p > 0)
+    both = (g_p > 0) & (w_p > 0) & (h_p > 0)
     same = np.array([np.abs(w_d[i] - g_d[i]).sum() / np.abs(g_d[i]).sum()
                      for i in range(ntest)])
-    start_err = np.array([np.abs(prop[i] - g_d[i]).sum()
-                          / np.abs(g_d[i]).sum() for i in range(ntest)])
-    ratio = g_p[both] / np.maximum(w_p[both], 1)
+    ref = simpson_normalise(g_d, dq)
+
+    def err(d):
+        return np.array([np.abs(d[i] - ref[i]).sum() / np.abs(ref[i]).sum()
+                         for i in range(ntest)])
+
+    def med(v):
+        return float(np.median(v)) if both.any() else None
+
     out = {
         "grid": n, "steps_per_period": spt, "tolerance_per_period": tol,
         "train_tolerance_per_period": tol_train or tol, "iters": iters,
         "train_samples": int(ntrain), "train_converged": int(ok.sum()),
-        "test_samples": int(ntest), "test_converged_both": int(both.sum()),
+        "residual_scale": scale,
+        "test_samples": int(ntest), "test_converged_all": int(both.sum()),
         "test_converged_gaussian": int((g_p > 0).sum()),
+        "test_converged_potential_well": int((h_p > 0).sum()),
         "test_converged_warm": int((w_p > 0).sum()),
         "train_loss_first": hist[0], "train_loss_last": hist[-1],
-        "periods_gaussian_median": float(np.median(g_p[both])) if both.any()
-        else None,
-        "periods_warm_median": float(np.median(w_p[both])) if both.any()
-        else None,
-        "speedup_median": float(np.median(ratio)) if both.any() else None,
+        "periods_gaussian_median": med(g_p[both]),
+        "periods_potential_well_median": med(h_p[both]),
+        "periods_warm_median": med(w_p[both]),
+        "speedup_potential_well_median":
+            med(g_p[both] / np.maximum(h_p[both], 1)),
+        "speedup_median": med(g_p[both] / np.maximum(w_p[both], 1)),
         "speedup_total": float(g_p[both].sum() / max(w_p[both].sum(), 1))
         if both.any() else None,
-        "proposal_l1_median": float(np.median(start_err)),
+        "potential_well_l1_median": float(np.median(err(base))),
+        "proposal_l1_median": float(np.median(err(prop))),
         "same_equilibrium_l1_max": float(same[both].max()) if both.any()
         else None,
     }

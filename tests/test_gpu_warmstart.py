@@ -1,10 +1,11 @@
 """Learned warm start: the library's forward/backward kernels against the
 float64 numpy restatement (oracle/warmstart_ref.py), then a small
-experiment at 128x128: trained on solver equilibria, the proposals must
-reach the same equilibrium as the Gaussian start in fewer periods.  Both
-runs stop when the profile changes by less than 1e-5 per period, which
-leaves each within about a damping time of that change (~1e-3) of the
-fixed point: the two end states must agree to relative L1 <= 3e-3.
+experiment at 128x128: the potential-well state plus the correction
+trained on solver equilibria must reach the same equilibrium as the
+Gaussian start in fewer periods.  Both runs stop when the profile changes
+by less than 1e-5 per period, which leaves each within about a damping
+time of that change (~1e-3) of the fixed point: the two end states must
+agree to relative L1 <= 3e-3.
 
 Gradient tolerance: each gradient within 2e-3 of its largest entry (BF16
 weights are used exactly on both sides; the GPU sums in FP32)."""
@@ -42,8 +43,9 @@ def test_ws_small_experiment(gpu_ctx):
     res, _ = W.experiment(gpu_ctx, n=128, spt=500, ntrain=192, ntest=24,
                           iters=1500, max_periods=200, seed=11)
     print(res)
-    assert res["train_loss_last"] < 0.05 * res["train_loss_first"]
-    assert res["test_converged_both"] >= 0.8 * res["test_converged_gaussian"]
+    assert res["train_loss_last"] < 0.5 * res["train_loss_first"]
+    assert res["test_converged_all"] >= 0.8 * res["test_converged_gaussian"]
     assert res["same_equilibrium_l1_max"] <= 3e-3
-    assert res["proposal_l1_median"] <= 1e-2
-    assert res["speedup_median"] >= 1.3
+    assert res["proposal_l1_median"] <= 5e-3
+    assert res["speedup_median"] >= 1.5
+    assert res["periods_warm_median"] < res["periods_gaussian_median"]
