@@ -540,8 +540,13 @@ def main():
     a_in = np.ctypeslib.as_array((C.c_float * cells).from_address(hin.value))
     a_out = np.ctypeslib.as_array((C.c_float * cells).from_address(hout.value))
     a_in[:] = batch.download()
-    prof = np.zeros(batch.rows, np.float32)
-    fill = np.zeros(NB, np.float32)
+    hprof = C.c_void_p()
+    hfill = C.c_void_p()
+    _lib.check(L.vfps_host_alloc(ctx.handle, batch.rows * 4, C.byref(hprof)))
+    _lib.check(L.vfps_host_alloc(ctx.handle, NB * 4, C.byref(hfill)))
+    prof = np.ctypeslib.as_array(
+        (C.c_float * batch.rows).from_address(hprof.value))
+    fill = np.ctypeslib.as_array((C.c_float * NB).from_address(hfill.value))
     batch.run(a_in, args.e2e_steps, a_out, prof, fill)
     reps = max(3, 2000 // args.e2e_steps)
     t = time.perf_counter()
@@ -549,6 +554,9 @@ def main():
         batch.run(a_in, args.e2e_steps, a_out, prof, fill)
     e2e_s = (time.perf_counter() - t) / reps
     e2e_value = cells * args.e2e_steps * world / e2e_s
+    del a_in, a_out, prof, fill
+    for h in (hin, hout, hprof, hfill):
+        _lib.check(L.vfps_host_free(ctx.handle, h))
 
     # plain one-map-per-launch loop, one bunch at a time
     plain = PlainSolver(ctx, p, chain=0, wake_impedance=z,

@@ -1018,10 +1018,40 @@ extern "C" int vfps_batch_step(vfps_batch* b, uint64_t nsteps)
 
 namespace {
 
+// per-bunch arrays of n rows (profiles, wakes) without gaps between bunches
+bool rows_packed(const vfps_batch* b)
+{
+    size_t off = 0;
+    for (const auto& B : b->hb) {
+        if (B.prof_off != off) {
+            return false;
+        }
+        off += B.n;
+    }
+    return true;
+}
+
 void copy_packed(vfps_batch* b, float* host, bool to_host, bool profiles,
                  const float* src_dev = nullptr)
 {
     cudaStream_t st = b->ctx->stream;
+    if (profiles && rows_packed(b)) {
+        // one copy instead of one per bunch (small copies into pageable
+        // memory each cost a staged, synchronous transfer)
+        const float* dev = src_dev ? src_dev : b->prof[b->cur].p;
+        size_t rows = 0;
+        for (const auto& B : b->hb) {
+            rows += B.n;
+        }
+        if (to_host) {
+            VFPS_CUDA(cudaMemcpyAsync(host, dev, rows * 4,
+                                      cudaMemcpyDeviceToHost, st));
+        } else {
+            VFPS_CUDA(cudaMemcpyAsync(const_cast<float*>(dev), host, rows * 4,
+                                      cudaMemcpyHostToDevice, st));
+        }
+        return;
+    }
     size_t off = 0;
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];

@@ -184,11 +184,12 @@ __device__ __forceinline__ void toeplitz_partials(const float* P,
         const int k = bidx > 0 ? bidx : 0;
         w[0] = W[k + (k >> 3)];
     }
-    float* pr = partial + size_t(q) * n + x;
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-        pr[j] = acc[j];
-    }
+    // two 16-byte stores (partial starts 16-byte aligned: 13n bytes into
+    // the shared memory for n >= 64): a stride of 8 floats between lanes
+    // costs 8 wavefronts per store instead of 8 scalar 8-way conflicts
+    float4* pr = reinterpret_cast<float4*>(partial + size_t(q) * n + x);
+    pr[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+    pr[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
 }
 
 // W[k + k/8] = w[(k - (n-1)) mod nmax] for k < 2n - 1 (the layout that
