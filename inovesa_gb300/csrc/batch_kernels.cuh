@@ -1174,33 +1174,48 @@ __device__ __forceinline__ void drift2(const float* ring, const RingMap& m,
 {
     const int4 sh = __ldg(reinterpret_cast<const int4*>(W + 4 * n + y));
     if (sh.x == sh.y && sh.y == sh.z && sh.z == sh.w) {
+        // packed FP32 (two lanes of 4 columns per instruction; each
+        // component rounds like fmaf / a plain product)
         float4 wp = make_float4(0.f, 0.f, 0.f, 0.f);
+        float2 a0 = make_float2(0.f, 0.f), b0 = a0, a1 = a0, b1 = a0;
 #pragma unroll
         for (int j = 0; j < 5; j++) {
             const float4 v = *reinterpret_cast<const float4*>(
                 ring + size_t(m.slot(X0 + sh.x + j, rb)) * rs + APAD + y);
-            const float vv[4] = {v.x, v.y, v.z, v.w};
+            const float2 va = make_float2(v.x, v.y);
+            const float2 vb = make_float2(v.z, v.w);
             float4 wj = wp;
             if (j < 4) {
                 wj = __ldg(reinterpret_cast<const float4*>(W + j * n + y));
             }
-            const float wc[4] = {wj.x, wj.y, wj.z, wj.w};
-            const float pc[4] = {wp.x, wp.y, wp.z, wp.w};
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-                if (j == 0) {
-                    d0[c] = wc[c] * vv[c];
-                } else if (j < 4) {
-                    d0[c] = fmaf(wc[c], vv[c], d0[c]);
-                }
-                if (j == 1) {
-                    d1[c] = pc[c] * vv[c];
-                } else if (j > 1) {
-                    d1[c] = fmaf(pc[c], vv[c], d1[c]);
-                }
+            const float2 wa = make_float2(wj.x, wj.y);
+            const float2 wb = make_float2(wj.z, wj.w);
+            const float2 pa = make_float2(wp.x, wp.y);
+            const float2 pb = make_float2(wp.z, wp.w);
+            if (j == 0) {
+                a0 = __fmul2_rn(wa, va);
+                b0 = __fmul2_rn(wb, vb);
+            } else if (j < 4) {
+                a0 = __ffma2_rn(wa, va, a0);
+                b0 = __ffma2_rn(wb, vb, b0);
+            }
+            if (j == 1) {
+                a1 = __fmul2_rn(pa, va);
+                b1 = __fmul2_rn(pb, vb);
+            } else if (j > 1) {
+                a1 = __ffma2_rn(pa, va, a1);
+                b1 = __ffma2_rn(pb, vb, b1);
             }
             wp = wj;
         }
+        d0[0] = a0.x;
+        d0[1] = a0.y;
+        d0[2] = b0.x;
+        d0[3] = b0.y;
+        d1[0] = a1.x;
+        d1[1] = a1.y;
+        d1[2] = b1.x;
+        d1[3] = b1.y;
     } else {
         // a shift boundary inside the 4 columns: column by column
         const int shv[4] = {sh.x, sh.y, sh.z, sh.w};
