@@ -359,6 +359,20 @@ VFPS_API int vfps_batch_upload(vfps_batch* batch, const float* density);
 VFPS_API int vfps_batch_get_profiles(vfps_batch* batch, float* profiles);
 VFPS_API int vfps_batch_get_filling(vfps_batch* batch, double* filling);
 VFPS_API int vfps_batch_get_wake(vfps_batch* batch, float* wake);
+/* Multi-bunch beams (src/main.cpp:248-321, src/PS/ElectricField.cpp:
+ * 255-263): bunches with the same beam[i] > 0 share one padded profile,
+ * bunch i at bucket[i] * spacing_bins, so each one's wake carries the
+ * other members' fields (circular in the impedance's nfreqs, like the
+ * reference's FFT); beam[i] == 0 leaves bunch i alone.  Members must share
+ * mesh size, impedance and wake scaling (that of the beam's total
+ * current).  filling[nb] (optional): each bunch's share of the charge
+ * (the reference's filling_set); the current densities are normalised to
+ * it.  The tensor-core wake (vfps_batch_set_wake_mode 1) has no coupling
+ * and is switched off; the potential-well start uses each bunch's own
+ * field only. */
+VFPS_API int vfps_batch_set_beams(vfps_batch* batch, const uint32_t* beam,
+                                  const uint32_t* bucket,
+                                  uint32_t spacing_bins, const float* filling);
 /* Replace the density of every chain-0 bunch with the stationary state of
  * its solver step below the instability threshold, and refresh profiles
  * and filling (as vfps_batch_upload does).  The reference names this

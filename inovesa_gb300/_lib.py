@@ -149,6 +149,7 @@ SIGNATURES = {
     "vfps_batch_get_filling": [P, DP],
     "vfps_batch_get_wake": [P, FP],
     "vfps_batch_potential_well": [P, C.c_uint32, C.c_float, FP],
+    "vfps_batch_set_beams": [P, U32P, U32P, C.c_uint32, FP],
     "vfps_batch_info": [P, U32P, U32P],
     "vfps_batch_kernel_times": [P, u32, FP],
     "vfps_charge_noalloc": [P, P, u32, u32, flt, DP],

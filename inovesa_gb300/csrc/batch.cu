@@ -73,6 +73,9 @@ struct vfps_batch {
     // wake potentials on the tensor cores (k_wake_tc) instead of inside
     // k_bwake: Toeplitz planes per (impedance, mesh size) and bunch tiles
     int wake_tc = 0;
+    DevBuf<BeamDev> beams;     // per bunch: its beam (default: alone)
+    DevBuf<uint32_t> members;  // bunches grouped by beam
+    bool coupled = false;      // some beam has more than one bunch
     DevBuf<float> tplanes;
     DevBuf<TcGroup> tcg;
     DevBuf<uint32_t> tclist;
@@ -158,8 +161,9 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             VFPS_CUDA(cudaEventRecord(ev[i], st));
         }
     };
-    // P[n], padded W[2n + n/4], partial sums [Q][n] with Q n = 8 THREADS
-    const size_t wsm = (3 * size_t(b->max_n) + b->max_n / 4 + 8 * THREADS)
+    // P[n], padded W[2n + n/4], partial sums [Q][n] with Q n = 8 THREADS,
+    // a coupled beam's wake [n] and member profile [n]
+    const size_t wsm = (5 * size_t(b->max_n) + b->max_n / 4 + 8 * THREADS)
                        * sizeof(float);
     mark(0);
     const bool tc = b->wake_tc && b->tc_groups > 0;
@@ -172,8 +176,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     }
     k_bwake<<<b->nb, THREADS, wsm, st>>>(
         b->bd.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p, b->wake.p,
-        b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p,
-        b->ctx->d_status, tc ? 1 : 0);
+        b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p, b->beams.p,
+        b->members.p, b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
     if (!b->htiles[TL_RING].empty()) {
@@ -865,6 +869,16 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         put(b->dwt, dwt);
         put(b->pw, pws);
         put(b->pwtab, pwtab);
+        {
+            std::vector<BeamDev> beams(nb);
+            std::vector<uint32_t> members(nb);
+            for (uint32_t i = 0; i < nb; i++) {
+                beams[i] = BeamDev{i, 1u, 0, 0u};
+                members[i] = i;
+            }
+            put(b->beams, beams);
+            put(b->members, members);
+        }
         b->wt.alloc(std::max<size_t>(wt.size(), 1));
         for (uint32_t k = 0; k < nimp; k++) {
             if (wt_off[k] != 0xffffffffu) {
@@ -1302,9 +1316,88 @@ extern "C" int vfps_batch_kernel_times(vfps_batch* b, uint32_t nsteps,
     });
 }
 
+extern "C" int vfps_batch_set_beams(vfps_batch* b, const uint32_t* beam,
+                                    const uint32_t* bucket,
+                                    uint32_t spacing_bins,
+                                    const float* filling)
+{
+    if (!b || !beam || !bucket) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    return bguard(b->ctx, [&] {
+        const uint32_t nb = b->nb;
+        std::map<uint32_t, std::vector<uint32_t>> groups;
+        for (uint32_t i = 0; i < nb; i++) {
+            if (beam[i] != 0) {
+                groups[beam[i]].push_back(i);
+            }
+            VFPS_REQUIRE(!filling || filling[i] >= 0.f,
+                         "fillings must not be negative");
+        }
+        std::vector<BeamDev> beams(nb);
+        std::vector<uint32_t> members;
+        bool coupled = false;
+        for (uint32_t i = 0; i < nb; i++) {
+            if (beam[i] == 0) {
+                beams[i] = BeamDev{static_cast<uint32_t>(members.size()), 1u,
+                                   static_cast<int32_t>(bucket[i]),
+                                   spacing_bins};
+                members.push_back(i);
+            }
+        }
+        for (const auto& g : groups) {
+            const auto& idx = g.second;
+            const BDev& B0 = b->hb[idx[0]];
+            for (uint32_t j : idx) {
+                const BDev& B = b->hb[j];
+                VFPS_REQUIRE(B.n == B0.n && B.wt_off == B0.wt_off
+                                 && B.nmax == B0.nmax
+                                 && (B.flags & F_WAKE) == (B0.flags & F_WAKE)
+                                 && B.wakescale == B0.wakescale,
+                             "bunches of one beam need the same mesh, "
+                             "impedance and wake scaling");
+            }
+            const uint32_t first = static_cast<uint32_t>(members.size());
+            for (uint32_t j : idx) {
+                beams[j] = BeamDev{first, static_cast<uint32_t>(idx.size()),
+                                   static_cast<int32_t>(bucket[j]),
+                                   spacing_bins};
+            }
+            members.insert(members.end(), idx.begin(), idx.end());
+            coupled = coupled || idx.size() > 1;
+        }
+        cudaStream_t st = b->ctx->stream;
+        VFPS_CUDA(cudaStreamSynchronize(st));
+        VFPS_CUDA(cudaMemcpy(b->beams.p, beams.data(), nb * sizeof(BeamDev),
+                             cudaMemcpyHostToDevice));
+        VFPS_CUDA(cudaMemcpy(b->members.p, members.data(),
+                             nb * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        b->coupled = coupled;
+        if (filling) {
+            // the reference's filling_set: normalise every bunch to it
+            // (src/PS/PhaseSpace.cpp:342-372)
+            for (uint32_t i = 0; i < nb; i++) {
+                b->hb[i].fillset = filling[i];
+            }
+            VFPS_CUDA(cudaMemcpy(b->bd.p, b->hb.data(), nb * sizeof(BDev),
+                                 cudaMemcpyHostToDevice));
+            project_all(b, b->cur);
+            integrate_all(b, b->cur, 0);
+            integrate_all(b, b->cur, 1);
+            project_all(b, b->cur);
+            integrate_all(b, b->cur, 0);
+        }
+        if (coupled && b->wake_tc) {
+            b->wake_tc = 0;   // the tensor-core sum has no coupling
+        }
+        make_graphs(b);
+        VFPS_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
 extern "C" int vfps_batch_set_wake_mode(vfps_batch* b, int mode)
 {
-    if (!b || (mode != 0 && mode != 1)) {
+    if (!b || (mode != 0 && mode != 1) || (mode == 1 && b->coupled)) {
         return VFPS_ERR_INVALID_ARGUMENT;
     }
     return bguard(b->ctx, [&] {

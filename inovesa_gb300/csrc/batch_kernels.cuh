@@ -47,6 +47,16 @@ struct __align__(16) Tile {
 static_assert(sizeof(BDev) == 96 && sizeof(Tile) == 16,
               "host and device share these layouts");
 
+// the beam of a bunch: bunches of one beam share a padded profile (their
+// buckets spacing mesh cells apart, src/PS/ElectricField.cpp:255-263), so
+// each one's wake carries the others' fields
+struct BeamDev {
+    uint32_t first;    // its members in the member list
+    uint32_t count;    // 1: the bunch alone
+    int32_t bucket;    // bucket number of the bunch
+    uint32_t spacing;  // mesh cells between neighbouring buckets
+};
+
 // log2 of seg = n / 8 lanes per row (n a power of two): the lane splits
 // below are shifts and masks instead of divisions by a runtime value
 __device__ __forceinline__ int lg_seg(int n)
@@ -192,14 +202,18 @@ __device__ __forceinline__ void toeplitz_partials(const float* P,
     pr[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
 }
 
-// W[k + k/8] = w[(k - (n-1)) mod nmax] for k < 2n - 1 (the layout that
-// toeplitz_partials reads; |k - (n-1)| < n <= nmax / 2)
+// W[k + k/8] = w[(delta + k - (n-1)) mod nmax] for k < 2n - 1 (the layout
+// that toeplitz_partials reads): the field at distance delta + x - m of a
+// source cell m on row x (delta: the distance between two bunches' buckets
+// in the padded profile, 0 for a bunch's own field)
 __device__ __forceinline__ void load_toeplitz(const float* __restrict__ w,
-                                              int nmax, int n, float* W)
+                                              int nmax, int n, float* W,
+                                              long long delta = 0)
 {
     for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
-        const int d = k - (n - 1);
-        W[k + (k >> 3)] = w[d < 0 ? d + nmax : d];
+        long long d = (delta + k - (n - 1)) % nmax;
+        d += d < 0 ? nmax : 0;
+        W[k + (k >> 3)] = w[d];
     }
 }
 
@@ -214,7 +228,9 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         const float* __restrict__ pin, float* __restrict__ wake,
         RowInfo* __restrict__ rinfo, float* __restrict__ factor,
         double* __restrict__ filling, unsigned long long* __restrict__ tickets,
-        int* __restrict__ status, int wake_ready)
+        const BeamDev* __restrict__ beams,
+        const uint32_t* __restrict__ members, int* __restrict__ status,
+        int wake_ready)
 {
     extern __shared__ float4 wsm4[];
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
@@ -237,9 +253,13 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     const bool has_wake = B.flags & F_WAKE;
     // wake_ready: the tensor-core kernel has written this step's wake
     const bool sum_here = has_wake && !wake_ready;
+    // the bunch's own field (a coupled beam reloads it per member; not
+    // waiting for the beam record keeps this load off its latency)
     if (sum_here) {
         load_toeplitz(wt + B.wt_off, int(B.nmax), n, W);
     }
+    const BeamDev Mb = beams[b];
+    const bool coupled = Mb.count > 1;
     // loads for the later phases, issued now
     const float* ws = tabs + B.tab_off + TAB_WS * n;
     const int x0 = threadIdx.x;
@@ -271,8 +291,37 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     }
     float* partial = W + 2 * n + (n >> 2);   // [Q][n], Q n = 8 THREADS
     const int Q = THREADS / (n >> 3);
-    if (sum_here) {
+    float* acc = partial + 8 * THREADS;      // coupled beams: wake [n]
+    float* Pm = acc + n;                     // and a member's profile [n]
+    if (sum_here && !coupled) {
         toeplitz_partials(P, W, partial, n);
+    } else if (sum_here) {
+        // the fields of every member of the beam (this bunch included) at
+        // their bucket distances
+        for (int x = threadIdx.x; x < n; x += THREADS) {
+            acc[x] = 0.f;
+        }
+        for (uint32_t k = 0; k < Mb.count; k++) {
+            const uint32_t b2 = members[Mb.first + k];
+            const BDev B2 = bd[b2];
+            const long long delta = (long long)(Mb.bucket - beams[b2].bucket)
+                                    * Mb.spacing;
+            __syncthreads();   // the previous member's W, Pm, partial read
+            for (int i = threadIdx.x; i < n; i += THREADS) {
+                Pm[i] = pin[B2.prof_off + i];
+            }
+            load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, delta);
+            __syncthreads();
+            toeplitz_partials(Pm, W, partial, n);
+            __syncthreads();
+            for (int x = threadIdx.x; x < n; x += THREADS) {
+                float sum = 0.f;
+                for (int q = 0; q < Q; q++) {
+                    sum += partial[size_t(q) * n + x];
+                }
+                acc[x] += sum;   // read back by this thread only
+            }
+        }
     }
     __syncthreads();   // partial sums, per-warp integrals and ticket_s
     FF tot = FF{0.f, 0.f};
@@ -310,8 +359,12 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         float v = 0.f;
         if (sum_here) {
             float sum = 0.f;
-            for (int k = 0; k < Q; k++) {
-                sum += partial[size_t(k) * n + x];
+            if (coupled) {
+                sum = acc[x];
+            } else {
+                for (int k = 0; k < Q; k++) {
+                    sum += partial[size_t(k) * n + x];
+                }
             }
             v = __fmul_rn(B.wakescale, sum);
             wake[B.prof_off + x] = v;

@@ -1,6 +1,7 @@
-"""Plain solver loop: one bunch, one map per launch, the reference's own
-sequence of calls (src/main.cpp:469-760 for the set-up, :948-1053 for the
-step).  chain 0 is main.cpp's loop; chain 1 replaces the RF kick and
+"""Plain solver loop: one map per launch, the reference's own sequence of
+calls (src/main.cpp:469-760 for the set-up, :948-1053 for the step), for
+one bunch or one multi-bunch beam (fillings per bunch, bucket numbers and
+their spacing, src/main.cpp:248-321).  chain 0 is main.cpp's loop; chain 1 replaces the RF kick and
 drift by a RotationMap (the scheme of test/TestRotationMap.cpp).
 """
 from . import vfps as V
@@ -9,10 +10,14 @@ from . import vfps as V
 class PlainSolver:
     def __init__(self, ctx, p, chain=0, Ib=None, wake_impedance=None,
                  csr_impedance=None, it=None, clamp=False, data=None,
-                 resume_step=None):
-        """data: initial density [n][n] (else the Gaussian); with
-        resume_step, data is a saved state that continues at that step
-        (not normalised again, renormalisation schedule kept)."""
+                 resume_step=None, fillings=None, buckets=None,
+                 spacing=None):
+        """data: initial density [n][n] or [nb][n][n] (else the Gaussian);
+        with resume_step, data is a saved state that continues at that
+        step (not normalised again, renormalisation schedule kept).
+        fillings: each bunch's share of the charge (default one bunch);
+        buckets, spacing: bucket numbers and mesh cells between buckets of
+        a multi-bunch beam (default bucket 0, the derived spacing)."""
         o = p["opts"]
         self.p, self.chain = p, chain
         n = p["ps_bins"]
@@ -20,8 +25,11 @@ class PlainSolver:
         ib = p["Ib"] if Ib is None else Ib
         self.renormalize = int(o["RenormalizeCharge"])
         a = p["axes"]
+        fill = [1.0] if fillings is None else [float(f) for f in fillings]
+        self.buckets = [0] * len(fill) if buckets is None else list(buckets)
+        spacing = p["spacing_bins"] if spacing is None else int(spacing)
         self.t1 = V.PhaseSpace(a[0], a[1], a[2], a[3], a[4], a[5], ctx,
-                               ib / p["f_rev"], ib, [1.0],
+                               ib / p["f_rev"], ib, fill,
                                o["InitialDistZoom"], data, n=n)
         if self.renormalize >= 0 and resume_step is None:
             self.t1.updateXProjection()
@@ -34,7 +42,7 @@ class PlainSolver:
         self.wkm = None
         if wake_impedance is not None:
             self.wake_field = V.ElectricField.wake(
-                self.t1, wake_impedance, [0], p["spacing_bins"], ctx,
+                self.t1, wake_impedance, self.buckets, spacing, ctx,
                 p["f_rev"], p["revolutionpart"], ib, p["E0"], p["sE"],
                 p["dt"])
         if chain == 0:
@@ -70,7 +78,8 @@ class PlainSolver:
             self.fpm = V.Identity(self.t3, self.t1)
         self.rdtn = None
         if csr_impedance is not None:
-            self.rdtn = V.ElectricField(self.t1, csr_impedance, [0], 0, ctx,
+            self.rdtn = V.ElectricField(self.t1, csr_impedance, self.buckets,
+                                        0, ctx,
                                         p["f_rev"], p["revolutionpart"])
         self.simulationstep = 0 if resume_step is None else int(resume_step)
 
@@ -97,8 +106,8 @@ class PlainSolver:
             self.t1.updateXProjection()
             self.simulationstep += 1
 
-    def density(self):
-        return self.t1.getData()[0]
+    def density(self, b=0):
+        return self.t1.getData()[b]
 
-    def profile(self):
-        return self.t1.getProjection(0)[0]
+    def profile(self, b=0):
+        return self.t1.getProjection(0)[b]

@@ -707,6 +707,25 @@ class BunchBatch(_Handle):
         _, off = self.layout(b)
         return self.profiles()[off:off + int(self.descs[b].n)]
 
+    def set_beams(self, beam, bucket, spacing_bins, filling=None):
+        """Couple bunches into multi-bunch beams: equal beam ids > 0 share
+        one padded profile (bunch i at bucket[i] * spacing_bins); filling
+        (optional) is each bunch's share of the charge."""
+        nb = len(self.descs)
+        be = np.ascontiguousarray(beam, np.uint32)
+        bu = np.ascontiguousarray(bucket, np.uint32)
+        if be.size != nb or bu.size != nb:
+            raise InvalidArgument("beam and bucket need one entry per bunch")
+        fi = None
+        if filling is not None:
+            fi = np.ascontiguousarray(filling, np.float32)
+            if fi.size != nb:
+                raise InvalidArgument("filling needs one entry per bunch")
+        self._check(lib().vfps_batch_set_beams(
+            self._h, be.ctypes.data_as(_lib.U32P),
+            bu.ctypes.data_as(_lib.U32P), int(spacing_bins),
+            None if fi is None else _fptr(fi)))
+
     def potential_well(self, iterations=200, mix=0.5):
         """Replace every chain-0 density by the stationary state of its
         step below threshold (the Haissinski potential well written in the
