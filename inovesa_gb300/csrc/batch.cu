@@ -1,13 +1,18 @@
-// Batched solver step: many independent single-bunch simulations advanced
-// together (no reference counterpart; every bunch follows the reference
-// solver step, src/main.cpp:948-1053).  One step is two launches:
+// Batched solver step: many bunch simulations advanced together (no
+// reference counterpart; every bunch follows the reference solver step,
+// src/main.cpp:948-1053).  One step is k_bwake and, per tile list, one
+// maps kernel:
 //
 //  k_bwake   per bunch: the wake potential of every mesh row as the
 //            Toeplitz sum  wake[x] = s sum_m P[m] w[(x-m) mod nmax]  of the
-//            previous step's profile P (w built once per impedance in
-//            FP64), the charge integral (FP64), the renormalisation factor
-//            of this step and the step counter.
-//  k_bmaps0w  chain 0 (main.cpp's loop) on a tile of TX mesh rows: wake
+//            previous step's profiles P of its beam (w built once per
+//            impedance in FP64), the charge integral (compensated FP32),
+//            the renormalisation factor of this step, the y-kick stencils
+//            of chain-0 rows and a step ticket.
+//  k_bmaps0  chain 0 (main.cpp's loop) for meshes up to 256 rows: a
+//            persistent kernel streaming rows through a ring in shared
+//            memory (launched as a programmatic dependent of k_bwake).
+//  k_bmaps0w  chain 0 for wider meshes on a tile of TX mesh rows: wake
 //            y-kick and RF y-kick fused in registers, drift x-kick,
 //            Fokker-Planck, the new rows and their projections.
 //  k_bmaps1  chain 1 (rotation, wake y-kick, Fokker-Planck).
