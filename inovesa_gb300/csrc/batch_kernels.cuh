@@ -886,10 +886,12 @@ k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     __syncthreads();
 
     // each CTA walks a contiguous chunk of the tile list (tiles of a bunch
-    // are adjacent), so per-bunch column constants stay in registers
-    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
-    const uint32_t t_begin = blockIdx.x * per;
-    const uint32_t t_end = min(ntiles, t_begin + per);
+    // are adjacent), so per-bunch column constants stay in registers; the
+    // chunks differ by at most one tile
+    const uint32_t t_begin = uint32_t(uint64_t(blockIdx.x) * ntiles
+                                      / gridDim.x);
+    const uint32_t t_end = uint32_t(uint64_t(blockIdx.x + 1) * ntiles
+                                    / gridDim.x);
     uint32_t tid = t_begin;
     if (tid < t_end) {
         const Tile t = tiles[tid];
@@ -1421,10 +1423,13 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     __syncthreads();
 
     // each CTA walks a contiguous chunk of the tile list: tiles of a bunch
-    // are adjacent and in row order, so consecutive tiles share halo rows
-    const uint32_t per = (ntiles + gridDim.x - 1) / gridDim.x;
-    const uint32_t t_begin = blockIdx.x * per;
-    const uint32_t t_end = min(ntiles, t_begin + per);
+    // are adjacent and in row order, so consecutive tiles share halo rows;
+    // the chunks differ by at most one tile (no CTA left idle while others
+    // carry a whole extra tile)
+    const uint32_t t_begin = uint32_t(uint64_t(blockIdx.x) * ntiles
+                                      / gridDim.x);
+    const uint32_t t_end = uint32_t(uint64_t(blockIdx.x + 1) * ntiles
+                                    / gridDim.x);
 
     // ring state of the current and of the next tile: slot mapping and the
     // new rows [lo, hi) staged for it
