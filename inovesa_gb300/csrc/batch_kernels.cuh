@@ -1115,14 +1115,24 @@ template <int AL>
 __device__ __forceinline__ void kick7(const float* c, const RowInfo& ri,
                                       float* t2)
 {
+    // output pairs in packed FP32 (each component rounds like fmaf)
 #pragma unroll
-    for (int i = 0; i < 7; i++) {
-        float v = ri.a[0] * c[AL + i];
-        v = fmaf(ri.a[1], c[AL + i + 1], v);
-        v = fmaf(ri.a[2], c[AL + i + 2], v);
-        v = fmaf(ri.a[3], c[AL + i + 3], v);
-        t2[i] = v;
+    for (int i = 0; i < 6; i += 2) {
+        float2 v = __fmul2_rn(make_float2(ri.a[0], ri.a[0]),
+                              make_float2(c[AL + i], c[AL + i + 1]));
+#pragma unroll
+        for (int j = 1; j < 4; j++) {
+            v = __ffma2_rn(make_float2(ri.a[j], ri.a[j]),
+                           make_float2(c[AL + i + j], c[AL + i + j + 1]), v);
+        }
+        t2[i] = v.x;
+        t2[i + 1] = v.y;
     }
+    float v = ri.a[0] * c[AL + 6];
+    v = fmaf(ri.a[1], c[AL + 7], v);
+    v = fmaf(ri.a[2], c[AL + 8], v);
+    v = fmaf(ri.a[3], c[AL + 9], v);
+    t2[6] = v;
 }
 
 // Both y-kicks of the 4 cells y..y+3 of a staged row (mesh value of
@@ -1172,12 +1182,16 @@ __device__ __forceinline__ float4 ykick4(const float* row, int as, int n,
     }
     float o[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-        float v = ri.b[0] * t2[q];
-        v = fmaf(ri.b[1], t2[q + 1], v);
-        v = fmaf(ri.b[2], t2[q + 2], v);
-        v = fmaf(ri.b[3], t2[q + 3], v);
-        o[q] = v;
+    for (int q = 0; q < 4; q += 2) {
+        float2 v = __fmul2_rn(make_float2(ri.b[0], ri.b[0]),
+                              make_float2(t2[q], t2[q + 1]));
+#pragma unroll
+        for (int i = 1; i < 4; i++) {
+            v = __ffma2_rn(make_float2(ri.b[i], ri.b[i]),
+                           make_float2(t2[q + i], t2[q + i + 1]), v);
+        }
+        o[q] = v.x;
+        o[q + 1] = v.y;
     }
     return make_float4(o[0], o[1], o[2], o[3]);
 }
