@@ -373,6 +373,25 @@ VFPS_API int vfps_batch_get_wake(vfps_batch* batch, float* wake);
 VFPS_API int vfps_batch_set_beams(vfps_batch* batch, const uint32_t* beam,
                                   const uint32_t* bucket,
                                   uint32_t spacing_bins, const float* filling);
+/* CSR power of every bunch at recording steps (updateCSR,
+ * src/PS/ElectricField.cpp:133-184): the radiated power of the bunch's
+ * profile at the start of a step, the reference's sum over the half
+ * spectrum of the padded profile (its own impedance, cutoff and frequency
+ * axis), computed as the quadratic form of the profile with a Toeplitz
+ * kernel built once in FP64.  impedance[nb] indexes imps[nimp] (-1: no
+ * CSR for that bunch); fc[nb] the cutoff frequency (<= 0: none);
+ * freq_scale[nb] the "Hertz" scale of the frequency ruler (c / bunch
+ * length).  Steps with step % every == 0 are recorded into a ring of
+ * `capacity` slots; every == 0 switches recording off. */
+VFPS_API int vfps_batch_set_csr(vfps_batch* batch,
+                                const vfps_impedance* const* imps,
+                                uint32_t nimp, const int32_t* impedance,
+                                const double* fc, const double* freq_scale,
+                                uint32_t every, uint32_t capacity);
+/* The ring: power[capacity][nb] and steps[capacity], the step each slot
+ * holds (UINT64_MAX: not written yet). */
+VFPS_API int vfps_batch_get_csr(vfps_batch* batch, float* power,
+                                uint64_t* steps);
 /* Replace the density of every chain-0 bunch with the stationary state of
  * its solver step below the instability threshold, and refresh profiles
  * and filling (as vfps_batch_upload does).  The reference names this

@@ -62,6 +62,8 @@ FP = C.POINTER(C.c_float)
 DP = C.POINTER(C.c_double)
 U32P = C.POINTER(C.c_uint32)
 SZP = C.POINTER(C.c_size_t)
+I32P = C.POINTER(C.c_int32)
+U64P = C.POINTER(C.c_uint64)
 i32, u32, u64, sz, dbl, flt = (C.c_int, C.c_uint32, C.c_uint64, C.c_size_t,
                                C.c_double, C.c_float)
 
@@ -150,6 +152,9 @@ SIGNATURES = {
     "vfps_batch_get_wake": [P, FP],
     "vfps_batch_potential_well": [P, C.c_uint32, C.c_float, FP],
     "vfps_batch_set_beams": [P, U32P, U32P, C.c_uint32, FP],
+    "vfps_batch_set_csr": [P, PP, C.c_uint32, I32P, DP, DP, C.c_uint32,
+                           C.c_uint32],
+    "vfps_batch_get_csr": [P, FP, U64P],
     "vfps_batch_info": [P, U32P, U32P],
     "vfps_batch_kernel_times": [P, u32, FP],
     "vfps_charge_noalloc": [P, P, u32, u32, flt, DP],

@@ -81,6 +81,12 @@ struct vfps_batch {
     DevBuf<BeamDev> beams;     // per bunch: its beam (default: alone)
     DevBuf<uint32_t> members;  // bunches grouped by beam
     bool coupled = false;      // some beam has more than one bunch
+    // CSR power recording (vfps_batch_set_csr)
+    DevBuf<float> csrk;        // K tables
+    DevBuf<uint32_t> csroff;   // per bunch: its table or NO_CSR
+    DevBuf<float> csrpow;      // ring [cap][nb]
+    DevBuf<unsigned long long> csrsteps;   // ring [cap]
+    uint32_t csr_every = 0, csr_cap = 0;
     DevBuf<float> tplanes;
     DevBuf<TcGroup> tcg;
     DevBuf<uint32_t> tclist;
@@ -182,7 +188,10 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     k_bwake<<<b->nb, THREADS, wsm, st>>>(
         b->bd.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p, b->wake.p,
         b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p, b->beams.p,
-        b->members.p, b->ctx->d_status, tc ? 1 : 0);
+        b->members.p,
+        CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
+               b->csr_every, b->csr_cap},
+        b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
     if (!b->htiles[TL_RING].empty()) {
@@ -884,6 +893,13 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             put(b->beams, beams);
             put(b->members, members);
         }
+        {
+            const std::vector<uint32_t> none(nb, NO_CSR);
+            put(b->csroff, none);
+            b->csrk.alloc(1);
+            b->csrpow.alloc(1);
+            b->csrsteps.alloc(1);
+        }
         b->wt.alloc(std::max<size_t>(wt.size(), 1));
         for (uint32_t k = 0; k < nimp; k++) {
             if (wt_off[k] != 0xffffffffu) {
@@ -1396,6 +1412,123 @@ extern "C" int vfps_batch_set_beams(vfps_batch* b, const uint32_t* beam,
             b->wake_tc = 0;   // the tensor-core sum has no coupling
         }
         make_graphs(b);
+        VFPS_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+extern "C" int vfps_batch_set_csr(vfps_batch* b,
+                                  const vfps_impedance* const* imps,
+                                  uint32_t nimp, const int32_t* impedance,
+                                  const double* fc, const double* freq_scale,
+                                  uint32_t every, uint32_t capacity)
+{
+    if (!b || (every > 0 && (!imps || !impedance || !fc || !freq_scale
+                             || capacity == 0))) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    return bguard(b->ctx, [&] {
+        cudaStream_t st = b->ctx->stream;
+        VFPS_CUDA(cudaStreamSynchronize(st));
+        const uint32_t nb = b->nb;
+        std::vector<uint32_t> off(nb, NO_CSR);
+        std::vector<float> tabs;
+        if (every > 0) {
+            // one K table per (impedance, mesh, dq, cutoff, frequency scale)
+            std::map<std::string, uint32_t> seen;
+            std::vector<std::vector<float>> re(nimp);
+            for (uint32_t i = 0; i < nb; i++) {
+                if (impedance[i] < 0) {
+                    continue;
+                }
+                const uint32_t k = static_cast<uint32_t>(impedance[i]);
+                VFPS_REQUIRE(k < nimp && imps[k], "bunch names a missing "
+                             "CSR impedance");
+                const vfps_impedance* z = imps[k];
+                const BDev& B = b->hb[i];
+                const size_t nmax = z->nfreqs;
+                VFPS_REQUIRE(nmax >= B.n, "CSR impedance needs at least n "
+                             "frequencies");
+                const double dq = double(B.dq);
+                std::string key(reinterpret_cast<const char*>(&k), 4);
+                key.append(reinterpret_cast<const char*>(&B.n), 4);
+                key.append(reinterpret_cast<const char*>(&B.dq), 4);
+                key.append(reinterpret_cast<const char*>(&fc[i]), 8);
+                key.append(reinterpret_cast<const char*>(&freq_scale[i]), 8);
+                auto it = seen.find(key);
+                if (it != seen.end()) {
+                    off[i] = it->second;
+                    continue;
+                }
+                if (re[k].empty()) {
+                    std::vector<float> zz(2 * nmax);
+                    VFPS_CUDA(cudaMemcpy(zz.data(), z->z.p, zz.size() * 4,
+                                         cudaMemcpyDeviceToHost));
+                    re[k].resize(nmax);
+                    for (size_t f = 0; f < nmax; f++) {
+                        re[k][f] = zz[2 * f];
+                    }
+                }
+                // the frequency ruler 0 .. 1/dq over nmax points
+                // (src/PS/ElectricField.cpp:133-184)
+                const double df = (1.0 / dq) / double(nmax - 1);
+                std::vector<double> c(nmax / 2 + 1);
+                for (size_t f = 0; f <= nmax / 2; f++) {
+                    double r = dq * dq;
+                    if (fc[i] > 0) {
+                        const double u = freq_scale[i] * df * double(f)
+                                         / fc[i];
+                        r *= 1.0 - std::exp(-u * u);
+                    }
+                    c[f] = r * double(re[k][f]);
+                }
+                const uint32_t n = B.n;
+                off[i] = static_cast<uint32_t>(tabs.size());
+                seen.emplace(key, off[i]);
+                const double two_pi = 6.283185307179586476925286766559;
+                for (int64_t d = 1 - int64_t(n); d < int64_t(n); d++) {
+                    double sum = 0;
+                    for (size_t f = 0; f <= nmax / 2; f++) {
+                        // the angle reduced exactly before the cosine
+                        const int64_t r = (d * int64_t(f)) % int64_t(nmax);
+                        sum += c[f] * std::cos(two_pi * double(r)
+                                               / double(nmax));
+                    }
+                    tabs.push_back(static_cast<float>(df * sum));
+                }
+            }
+            b->csrk.alloc(std::max<size_t>(tabs.size(), 1));
+            if (!tabs.empty()) {
+                VFPS_CUDA(cudaMemcpy(b->csrk.p, tabs.data(), tabs.size() * 4,
+                                     cudaMemcpyHostToDevice));
+            }
+            b->csrpow.alloc(size_t(capacity) * nb);
+            VFPS_CUDA(cudaMemset(b->csrpow.p, 0, b->csrpow.bytes()));
+            b->csrsteps.alloc(capacity);
+            VFPS_CUDA(cudaMemset(b->csrsteps.p, 0xff, b->csrsteps.bytes()));
+        }
+        VFPS_CUDA(cudaMemcpy(b->csroff.p, off.data(), nb * 4,
+                             cudaMemcpyHostToDevice));
+        b->csr_every = every;
+        b->csr_cap = every > 0 ? capacity : 0;
+        make_graphs(b);
+        VFPS_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+extern "C" int vfps_batch_get_csr(vfps_batch* b, float* power,
+                                  uint64_t* steps)
+{
+    if (!b || !power || !steps || b->csr_every == 0) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    return bguard(b->ctx, [&] {
+        cudaStream_t st = b->ctx->stream;
+        VFPS_CUDA(cudaMemcpyAsync(power, b->csrpow.p,
+                                  size_t(b->csr_cap) * b->nb * 4,
+                                  cudaMemcpyDeviceToHost, st));
+        VFPS_CUDA(cudaMemcpyAsync(steps, b->csrsteps.p,
+                                  size_t(b->csr_cap) * 8,
+                                  cudaMemcpyDeviceToHost, st));
         VFPS_CUDA(cudaStreamSynchronize(st));
     });
 }

@@ -47,6 +47,23 @@ struct __align__(16) Tile {
 static_assert(sizeof(BDev) == 96 && sizeof(Tile) == 16,
               "host and device share these layouts");
 
+// CSR power recording of the batched step (src/PS/ElectricField.cpp:
+// 133-184): the power of a profile P is the quadratic form
+//   sum_{m,m'} P[m] P[m'] K(m - m'),
+//   K(d) = df sum_{i <= nmax/2} dq^2 c(f_i) Re Z[i] cos(2 pi i d / nmax),
+// c the cutoff factor 1 - exp(-(f/fc)^2) (1 without a cutoff): the same
+// number as the reference's sum of its spectrum over the half spectrum of
+// the padded profile, as one Toeplitz product and a dot product
+constexpr uint32_t NO_CSR = 0xffffffffu;
+struct CsrRec {
+    const float* k;              // K(d) for d = 1-n .. n-1, per table
+    const uint32_t* off;         // per bunch: its table (NO_CSR: none)
+    float* power;                // ring [cap][nb]
+    unsigned long long* steps;   // ring [cap]: the step in each slot
+    uint32_t every;              // record steps with step % every == 0
+    uint32_t cap;                // (every == 0: no recording)
+};
+
 // the beam of a bunch: bunches of one beam share a padded profile (their
 // buckets spacing mesh cells apart, src/PS/ElectricField.cpp:255-263), so
 // each one's wake carries the others' fields
@@ -229,8 +246,8 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         RowInfo* __restrict__ rinfo, float* __restrict__ factor,
         double* __restrict__ filling, unsigned long long* __restrict__ tickets,
         const BeamDev* __restrict__ beams,
-        const uint32_t* __restrict__ members, int* __restrict__ status,
-        int wake_ready)
+        const uint32_t* __restrict__ members, CsrRec csr,
+        int* __restrict__ status, int wake_ready)
 {
     extern __shared__ float4 wsm4[];
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
@@ -395,6 +412,52 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         }
         ri.pad[0] = ri.pad[1] = 0;
         rinfo[B.prof_off + x] = ri;
+    }
+    // CSR power of this step's profile (recording steps only; the same
+    // decision in every CTA)
+    if (csr.every == 0 || step % csr.every != 0) {
+        return;
+    }
+    const uint32_t koff = csr.off[b];
+    if (koff == NO_CSR) {
+        return;
+    }
+    __syncthreads();   // W and the partial sums of the wake are free
+    for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
+        W[k + (k >> 3)] = csr.k[koff + k];
+    }
+    __syncthreads();
+    toeplitz_partials(P, W, partial, n);
+    __syncthreads();
+    FF dot = FF{0.f, 0.f};
+    for (int x = threadIdx.x; x < n; x += THREADS) {
+        float v = 0.f;
+        for (int q = 0; q < Q; q++) {
+            v += partial[size_t(q) * n + x];
+        }
+        dot = ff_add(dot, ff_prod(P[x], v));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const FF t{__shfl_down_sync(0xffffffffu, dot.hi, o),
+                   __shfl_down_sync(0xffffffffu, dot.lo, o)};
+        dot = ff_add(dot, t);
+    }
+    __syncthreads();   // red[] was read by every thread above
+    if (lane == 0) {
+        red[warp] = make_float2(dot.hi, dot.lo);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        FF tot = FF{0.f, 0.f};
+        for (int w2 = 0; w2 < (THREADS >> 5); w2++) {
+            tot = ff_add(tot, FF{red[w2].x, red[w2].y});
+        }
+        const uint32_t slot = (step / csr.every) % csr.cap;
+        csr.power[size_t(slot) * gridDim.x + b] = tot.hi + tot.lo;
+        if (b == 0) {
+            csr.steps[slot] = step;
+        }
     }
 }
 

@@ -1,8 +1,9 @@
 """Plain solver loop: one map per launch, the reference's own sequence of
 calls (src/main.cpp:469-760 for the set-up, :948-1053 for the step), for
 one bunch or one multi-bunch beam (fillings per bunch, bucket numbers and
-their spacing, src/main.cpp:248-321).  chain 0 is main.cpp's loop; chain 1 replaces the RF kick and
-drift by a RotationMap (the scheme of test/TestRotationMap.cpp).
+their spacing, src/main.cpp:248-321).  chain 0 is main.cpp's loop; chain 1
+replaces the RF kick and drift by a RotationMap (the scheme of
+test/TestRotationMap.cpp).
 """
 from . import vfps as V
 

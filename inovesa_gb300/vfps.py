@@ -17,7 +17,8 @@ from ._lib import BunchDesc, InvalidArgument, VfpsError, check, lib
 
 __all__ = [
     "Context", "PhaseSpace", "RotationMap", "KickMap", "DriftMap",
-    "RFKickMap", "DynamicRFKickMap", "FokkerPlanckMap", "Identity", "WakePotentialMap",
+    "RFKickMap", "DynamicRFKickMap", "FokkerPlanckMap", "Identity",
+    "WakePotentialMap",
     "Impedance", "FreeSpaceCSR", "ParallelPlatesCSR", "ResistiveWall",
     "ConstImpedance", "CollimatorImpedance", "makeImpedance",
     "ElectricField", "BunchBatch", "BunchDesc", "InvalidArgument",
@@ -715,16 +716,53 @@ class BunchBatch(_Handle):
         be = np.ascontiguousarray(beam, np.uint32)
         bu = np.ascontiguousarray(bucket, np.uint32)
         if be.size != nb or bu.size != nb:
-            raise InvalidArgument("beam and bucket need one entry per bunch")
+            raise InvalidArgument(
+                1, "beam and bucket need one entry per bunch")
         fi = None
         if filling is not None:
             fi = np.ascontiguousarray(filling, np.float32)
             if fi.size != nb:
-                raise InvalidArgument("filling needs one entry per bunch")
+                raise InvalidArgument(1, "filling needs one entry per bunch")
         self._check(lib().vfps_batch_set_beams(
             self._h, be.ctypes.data_as(_lib.U32P),
             bu.ctypes.data_as(_lib.U32P), int(spacing_bins),
             None if fi is None else _fptr(fi)))
+
+    def set_csr(self, impedances, impedance, fc, freq_scale, every=1,
+                capacity=64):
+        """Record every bunch's CSR power (the reference's updateCSR) at
+        steps with step % every == 0 into a ring of `capacity` slots.
+        impedances: Impedance objects; impedance, fc, freq_scale: per bunch
+        (impedance -1: no CSR for that bunch); every=0 switches it off."""
+        nb = len(self.descs)
+        self._csr_imps = list(impedances)
+        hs = (C.c_void_p * max(1, len(self._csr_imps)))(
+            *[z.handle for z in self._csr_imps])
+        idx = np.ascontiguousarray(impedance, np.int32)
+        f = np.ascontiguousarray(fc, np.float64)
+        sc = np.ascontiguousarray(freq_scale, np.float64)
+        if idx.size != nb or f.size != nb or sc.size != nb:
+            raise InvalidArgument(
+                1, "impedance, fc and freq_scale need one entry per bunch")
+        self._check(lib().vfps_batch_set_csr(
+            self._h, hs, len(self._csr_imps), idx.ctypes.data_as(_lib.I32P),
+            f.ctypes.data_as(_lib.DP), sc.ctypes.data_as(_lib.DP),
+            int(every), int(capacity)))
+        self._csr_cap = int(capacity) if every else 0
+
+    def csr(self):
+        """(steps, power[len(steps)][nb]) of the recorded steps in order."""
+        nb = len(self.descs)
+        cap = getattr(self, "_csr_cap", 0)
+        if cap == 0:
+            raise InvalidArgument(1, "CSR recording is off")
+        power = np.empty((cap, nb), np.float32)
+        steps = np.empty(cap, np.uint64)
+        self._check(lib().vfps_batch_get_csr(
+            self._h, _fptr(power), steps.ctypes.data_as(_lib.U64P)))
+        ok = steps != np.uint64(0xffffffffffffffff)
+        order = np.argsort(steps[ok], kind="stable")
+        return steps[ok][order].astype(np.int64), power[ok][order]
 
     def potential_well(self, iterations=200, mix=0.5):
         """Replace every chain-0 density by the stationary state of its
