@@ -328,6 +328,45 @@ def other_workload(args):
         out["accuracy_steps"] = steps
         out["config"] = {"grid": n, "steps_per_period": spt, "S": S,
                          "chain": chain, "csr_every_step": csr}
+        if args.workload == "bursting":
+            # the batched step on the same bunch, and on a bursting scan of
+            # 32 such bunches (S log-spaced 0.8..1.6), with every bunch's
+            # CSR power recorded every step
+            def batched(currents):
+                descs = [P.fill_desc(V.BunchDesc(), p, 0,
+                                     Ib=p["Ib"] * c / S, impedance=0)
+                         for c in currents]
+                b = V.BunchBatch(ctx, descs, [z])
+                nbb = len(currents)
+                b.set_csr([zr], [0] * nbb, [p["fc"]] * nbb,
+                          [P.C / p["bl"]] * nbb, every=1, capacity=8)
+                b.step(args.warmup)
+                ctx.synchronize()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                b.step(args.steps)
+                e1.record(stream)
+                e1.synchronize()
+                return b, b.cells * args.steps / (e0.elapsed_time(e1) / 1e3)
+            b1, out["gpu_batched_one"] = batched([S])
+            _, out["gpu_batched_scan32"] = batched(
+                list(np.geomspace(0.8, 1.6, 32)))
+            b3, _ = batched([S])
+            before = b3.download().reshape(n, n).copy()
+            ref3 = oracle.Sim([d], Z=z.data(), data=before,
+                              dtype=np.float64)
+            b3.step(200)
+            ref3.step(200)
+            # shapes at equal charge (the oracle normalises the state it
+            # is given; the batch's charge has drifted by ~1e-5 by then)
+            want = ref3.density(0)
+            got = b3.density(0).astype(np.float64)
+            got *= want.sum() / got.sum()
+            out["batched_density_l1_vs_fp64"] = float(
+                np.abs(got - want).sum() / np.abs(want).sum())
+            out["batched_note"] = ("batched rates include the CSR power of "
+                                   "every bunch every step")
     else:
         rng = np.random.default_rng(4)
         nb, spt = 96, 2000
