@@ -70,6 +70,12 @@ VFPS_API void* vfps_stream(vfps_ctx* ctx);
 /* Device-side error word (bounded waits, watchdogs); 0 = none.  Reading it
  * synchronises; *code is cleared afterwards. */
 VFPS_API int vfps_device_status(vfps_ctx* ctx, int* code);
+/* No reference counterpart: exercises the failure path of the solver
+ * kernels' bounded waits without faulting the GPU.  One kernel waits on a
+ * barrier that nothing completes, gives up after limit_ns (at most 1 s)
+ * and sets the device status to VFPS_ERR_TIMEOUT; the context stays
+ * usable (read and clear the status with vfps_device_status). */
+VFPS_API int vfps_selftest_wait_timeout(vfps_ctx* ctx, uint64_t limit_ns);
 /* Pinned host buffers for asynchronous copies (no reference counterpart). */
 VFPS_API int vfps_host_alloc(vfps_ctx* ctx, size_t bytes, void** ptr);
 VFPS_API int vfps_host_free(vfps_ctx* ctx, void* ptr);

@@ -76,6 +76,7 @@ SIGNATURES = {
     "vfps_device_status": [P, C.POINTER(C.c_int)],
     "vfps_host_alloc": [P, sz, PP],
     "vfps_host_free": [P, P],
+    "vfps_selftest_wait_timeout": [P, C.c_uint64],
     "vfps_ps_create": [P, u32, u32, DP, dbl, dbl, FP, dbl, FP, PP],
     "vfps_ps_copy": [P, PP],
     "vfps_ps_destroy": [P],

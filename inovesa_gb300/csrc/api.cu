@@ -198,6 +198,40 @@ extern "C" int vfps_device_status(vfps_ctx* ctx, int* code)
     });
 }
 
+namespace {
+// One thread waits for the first phase of an mbarrier that nothing arrives
+// at, bounded by limit_ns like every wait of the solver kernels: the wait
+// gives up, records VFPS_ERR_TIMEOUT and the kernel returns (no copy in
+// flight, no tensor memory held).
+__global__ void k_wait_selftest(int* status, unsigned long long limit_ns)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        vfps::dev::mbar_init(&bar, 1);
+        vfps::dev::mbar_fence_init();
+        if (!vfps::dev::mbar_wait_bounded(&bar, 0, limit_ns)) {
+            atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
+        }
+    }
+}
+}  // namespace
+
+extern "C" int vfps_selftest_wait_timeout(vfps_ctx* ctx, uint64_t limit_ns)
+{
+    if (!ctx) {
+        return null_arg("ctx");
+    }
+    if (limit_ns == 0 || limit_ns > 1000000000ull) {
+        ctx->last_error = "limit must be in (0, 1 s]";
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    return guard(ctx, [&] {
+        k_wait_selftest<<<1, 32, 0, ctx->stream>>>(ctx->d_status, limit_ns);
+        VFPS_LAUNCHED();
+        VFPS_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
 extern "C" int vfps_host_alloc(vfps_ctx* ctx, size_t bytes, void** ptr)
 {
     if (!ctx || !ptr) {
