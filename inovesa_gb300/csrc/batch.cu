@@ -9,7 +9,8 @@
 //            impedance in FP64), the charge integral (compensated FP32),
 //            the renormalisation factor of this step, the y-kick stencils
 //            of chain-0 rows and a step ticket.
-//  k_bmaps0  chain 0 (main.cpp's loop) for meshes up to 256 rows: a
+//  k_bmaps0  chain 0 (main.cpp's loop) for meshes up to 256 rows and for
+//            512-row meshes (template: 2 or 4 column groups per lane): a
 //            persistent kernel streaming rows through a ring in shared
 //            memory (launched as a programmatic dependent of k_bwake).
 //  k_bmaps0w  chain 0 for wider meshes on a tile of TX mesh rows: wake
@@ -40,8 +41,10 @@
 using vfps::DevBuf;
 
 // ================================================================== host
-enum { TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_COUNT = 3 };
-constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel
+enum { TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_COUNT = 4 };
+constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel, G = 2
+constexpr int RING4_N = 512;      // the mesh of the ring kernel, G = 4
+constexpr int RTHREADS4 = 256;    // its CTA: 8 warps, one row each
 
 struct vfps_batch {
     vfps_ctx* ctx = nullptr;
@@ -49,7 +52,8 @@ struct vfps_batch {
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    // tile lists: TL_RING (chain 0, n <= 256), TL_ROT (chain 1), TL_WIDE
+    // tile lists: TL_RING (chain 0, n <= 256), TL_RING4 (chain 0, n = 512),
+    // TL_ROT (chain 1), TL_WIDE
     // (chain 0, n >= 512)
     std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
@@ -68,10 +72,12 @@ struct vfps_batch {
     // step tickets: every k_bwake CTA takes one, so step = tickets / nb
     DevBuf<unsigned long long> tickets;
     int cur = 0;               // buffer holding the current state
-    size_t smem[TL_COUNT] = {0, 0, 0};
+    size_t smem[TL_COUNT] = {};
     SmemR layoutR{};           // shared-memory regions of k_bmaps0
     Smem0 layout0{};           // shared-memory regions of k_bmaps0w
     unsigned gridR = 0;        // persistent CTAs of k_bmaps0
+    SmemR layoutR4{};          // the same for the 512-row ring kernel
+    unsigned gridR4 = 0;
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
@@ -194,30 +200,40 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
         b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
-    if (!b->htiles[TL_RING].empty()) {
-        // programmatic dependent launch: the CTAs zero their rings and set
-        // up their barriers while k_bwake runs, then wait for it to finish
-        // (griddepcontrol.wait) before they read or write device memory.
-        // Only this kernel is launched so: k_bwake CTAs launched early
-        // crowd onto the SMs that finish this kernel first, which is slower.
-        cudaLaunchAttribute pdl[1];
-        pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-        pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    // programmatic dependent launch of the first ring kernel: its CTAs zero
+    // their rings and set up their barriers while k_bwake runs, then wait
+    // for it to finish (griddepcontrol.wait) before they read or write
+    // device memory.  Only ring kernels are launched so: k_bwake CTAs
+    // launched early crowd onto the SMs that finish first, which is slower.
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    bool first_ring = true;
+    auto ring_launch = [&](auto kernel, int list, unsigned grid, int threads,
+                           const SmemR& layout) {
+        if (b->htiles[list].empty()) {
+            return;
+        }
         cudaLaunchConfig_t c = {};
-        c.gridDim = dim3(b->gridR);
-        c.blockDim = dim3(RTHREADS);
-        c.dynamicSmemBytes = b->smem[TL_RING];
+        c.gridDim = dim3(grid);
+        c.blockDim = dim3(threads);
+        c.dynamicSmemBytes = b->smem[list];
         c.stream = st;
         c.attrs = pdl;
-        c.numAttrs = 1;
+        c.numAttrs = first_ring ? 1 : 0;
+        first_ring = false;
         VFPS_CUDA(cudaLaunchKernelEx(
-            &c, k_bmaps0, (const BDev*)b->bd.p, (const Tile*)b->tiles[TL_RING].p,
-            static_cast<uint32_t>(b->htiles[TL_RING].size()),
+            &c, kernel, (const BDev*)b->bd.p, (const Tile*)b->tiles[list].p,
+            static_cast<uint32_t>(b->htiles[list].size()),
             (const float*)b->tabs.p, (const float*)b->dwt.p,
             (const RowInfo*)b->rinfo.p, (const float*)b->dens[from].p,
-            b->dens[to].p, b->prof[to].p, b->ctx->d_status, b->layoutR));
+            b->dens[to].p, b->prof[to].p, b->ctx->d_status, layout));
         VFPS_LAUNCHED();
-    }
+    };
+    ring_launch(k_bmaps0<2, RTHREADS>, TL_RING, b->gridR, RTHREADS,
+                b->layoutR);
+    ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
+                b->layoutR4);
     if (!b->htiles[TL_WIDE].empty()) {
         k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], st>>>(
             b->bd.p, b->tiles[TL_WIDE].p,
@@ -267,14 +283,16 @@ void build_tiles(vfps_batch* b, int tile_cells)
     int max_rows = 0;
     // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
-    int ring_rows = 0, ring_n = 0;
+    int ring_rows = 0, ring_n = 0, ring4_rows = 0;
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
         const int c = B.chain == 1 ? TL_ROT
-                      : (n <= RING_MAX_N ? TL_RING : TL_WIDE);
+                      : (n <= RING_MAX_N ? TL_RING
+                                         : (n == RING4_N ? TL_RING4
+                                                         : TL_WIDE));
         int tx = std::max(4, tile_cells / n);
-        if (c == TL_RING) {
+        if (c == TL_RING || c == TL_RING4) {
             // the ring holds two tiles with their halos: at most 32 staged
             // rows per tile keeps it at 64 slots
             tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
@@ -289,6 +307,8 @@ void build_tiles(vfps_batch* b, int tile_cells)
         if (c == TL_RING) {
             ring_rows = std::max(ring_rows, nr);
             ring_n = std::max(ring_n, n);
+        } else if (c == TL_RING4) {
+            ring4_rows = std::max(ring4_rows, nr);
         } else if (c == TL_WIDE) {
             a_floats = std::max(a_floats, size_t(nr) * astride0(n));
             b_floats = std::max(b_floats, size_t(nr) * n);
@@ -305,23 +325,32 @@ void build_tiles(vfps_batch* b, int tile_cells)
         *at = static_cast<uint32_t>(o);
         o = align16(o + bytes);
     };
-    if (!b->htiles[TL_RING].empty()) {
-        // the ring holds the staged rows of two tiles with their halos
-        SmemR& L = b->layoutR;
+    // the ring holds the staged rows of two tiles with their halos
+    auto ring_layout = [&](SmemR& L, int rows, int n) {
         int rb = 1;
-        while (rb < 2 * ring_rows) {
+        while (rb < 2 * rows) {
             rb *= 2;
         }
         L.rb = static_cast<uint32_t>(rb);
-        L.rs = static_cast<uint32_t>(astride0(ring_n));
+        L.rs = static_cast<uint32_t>(astride0(n));
         o = 0;
         take(&L.ring, size_t(rb) * L.rs * 4);
-        take(&L.s, size_t(ring_rows) * sizeof(RowInfo));
+        take(&L.s, size_t(rows) * sizeof(RowInfo));
         take(&L.bar, 2 * sizeof(uint64_t));
         L.total = static_cast<uint32_t>(o);
-        b->smem[TL_RING] = o;
-        b->gridR = persistent_grid(b, k_bmaps0, RTHREADS, o,
+        return o;
+    };
+    if (!b->htiles[TL_RING].empty()) {
+        b->smem[TL_RING] = ring_layout(b->layoutR, ring_rows, ring_n);
+        b->gridR = persistent_grid(b, k_bmaps0<2, RTHREADS>, RTHREADS,
+                                   b->smem[TL_RING],
                                    b->htiles[TL_RING].size());
+    }
+    if (!b->htiles[TL_RING4].empty()) {
+        b->smem[TL_RING4] = ring_layout(b->layoutR4, ring4_rows, RING4_N);
+        b->gridR4 = persistent_grid(b, k_bmaps0<4, RTHREADS4>, RTHREADS4,
+                                    b->smem[TL_RING4],
+                                    b->htiles[TL_RING4].size());
     }
     if (!b->htiles[TL_WIDE].empty()) {
         Smem0& L = b->layout0;
@@ -358,10 +387,14 @@ void upload_tiles(vfps_batch* b)
 {
     VFPS_REQUIRE(tiles_fit(b),
                  "tile of the largest mesh does not fit in shared memory");
-    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0,
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<2, RTHREADS>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
                                        b->smem[TL_RING], 1))));
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<4, RTHREADS4>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_RING4], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0w,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(

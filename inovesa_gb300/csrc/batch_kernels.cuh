@@ -1466,7 +1466,138 @@ __device__ __forceinline__ void fp_rows2(const float* d0, const float* d1,
     p1 = fmaf(4.f, po[1], 2.f * pe[1]);
 }
 
-__global__ void __launch_bounds__(RTHREADS, 4)
+// Drift x-kick of one output row and 4 columns from the ring: tap j of row
+// X reads staged row X + shift + j (the same taps and order as drift2's
+// first row).
+__device__ __forceinline__ void drift1(const float* ring, const RingMap& m,
+                                       int rb, int rs, int X, int y,
+                                       const float* __restrict__ W, int n,
+                                       float* d)
+{
+    const int4 sh = __ldg(reinterpret_cast<const int4*>(W + 4 * n + y));
+    if (sh.x == sh.y && sh.y == sh.z && sh.z == sh.w) {
+        // packed FP32 (each component rounds like fmaf / a plain product)
+        float2 a = make_float2(0.f, 0.f), c = a;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const float4 v = *reinterpret_cast<const float4*>(
+                ring + size_t(m.slot(X + sh.x + j, rb)) * rs + APAD + y);
+            const float4 w = __ldg(reinterpret_cast<const float4*>(
+                W + j * n + y));
+            const float2 va = make_float2(v.x, v.y);
+            const float2 vb = make_float2(v.z, v.w);
+            const float2 wa = make_float2(w.x, w.y);
+            const float2 wb = make_float2(w.z, w.w);
+            if (j == 0) {
+                a = __fmul2_rn(wa, va);
+                c = __fmul2_rn(wb, vb);
+            } else {
+                a = __ffma2_rn(wa, va, a);
+                c = __ffma2_rn(wb, vb, c);
+            }
+        }
+        d[0] = a.x;
+        d[1] = a.y;
+        d[2] = c.x;
+        d[3] = c.y;
+    } else {
+        // a shift boundary inside the 4 columns: column by column
+        const int shv[4] = {sh.x, sh.y, sh.z, sh.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float t[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                t[j] = ring[size_t(m.slot(X + shv[q] + j, rb)) * rs + APAD
+                            + y + q];
+            }
+            float v = W[y + q] * t[0];
+            v = fmaf(W[n + y + q], t[1], v);
+            v = fmaf(W[2 * n + y + q], t[2], v);
+            v = fmaf(W[3 * n + y + q], t[3], v);
+            d[q] = v;
+        }
+    }
+}
+
+// Fokker-Planck of one row whose 32 lanes own G groups of 4 columns each
+// (group g: columns g n/G + 4l .. +3), neighbours by shuffles; the
+// neighbour of group g left of lane 0 is group g-1 on lane 31 and right of
+// lane 31 group g+1 on lane 0 (none beyond the mesh).  Stores the row
+// (valid) and returns its Simpson-weighted sum in units of h03 (as
+// fp_rows2).
+template <int G>
+__device__ __forceinline__ float fp_row(const float (&d)[G][4], int l, int n,
+                                        const float* __restrict__ F,
+                                        float* o, bool valid)
+{
+    const int lp = (l + 1) & 31, lm = (l + 31) & 31;
+    const bool first = l == 0, last = l == 31;
+    float L0[G], L1[G], R0[G], R1[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        L0[g] = __shfl_sync(0xffffffffu, d[g][2], lm);
+        L1[g] = __shfl_sync(0xffffffffu, d[g][3], lm);
+        R0[g] = __shfl_sync(0xffffffffu, d[g][0], lp);
+        R1[g] = __shfl_sync(0xffffffffu, d[g][1], lp);
+    }
+    const int gw = n / G;
+    float pe = 0.f, po = 0.f;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        const int y = g * gw + 4 * l;
+        float f[5][4];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(
+                F + q * n + y));
+            f[q][0] = v.x;
+            f[q][1] = v.y;
+            f[q][2] = v.z;
+            f[q][3] = v.w;
+        }
+        float w[8];
+        w[0] = first ? (g > 0 ? L0[g > 0 ? g - 1 : 0] : 0.f) : L0[g];
+        w[1] = first ? (g > 0 ? L1[g > 0 ? g - 1 : 0] : 0.f) : L1[g];
+        w[6] = last ? (g < G - 1 ? R0[g < G - 1 ? g + 1 : g] : 0.f) : R0[g];
+        w[7] = last ? (g < G - 1 ? R1[g < G - 1 ? g + 1 : g] : 0.f) : R1[g];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            w[2 + c] = d[g][c];
+        }
+        float out[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            float v = f[0][c] * w[c];
+            v = fmaf(f[1][c], w[c + 1], v);
+            v = fmaf(f[2][c], w[c + 2], v);
+            v = fmaf(f[3][c], w[c + 3], v);
+            v = fmaf(f[4][c], w[c + 4], v);
+            out[c] = v;
+        }
+        if (valid) {
+            *reinterpret_cast<float4*>(o + y) =
+                make_float4(out[0], out[1], out[2], out[3]);
+        }
+        // Simpson weights along the row: even columns 2, odd 4, column 0
+        // and n - 1 one
+        float e = out[0] + out[2], od = out[1] + out[3];
+        if (g == 0 && first) {
+            e -= 0.5f * out[0];
+        }
+        if (g == G - 1 && last) {
+            od -= 0.75f * out[3];
+        }
+        pe += e;
+        po += od;
+    }
+    return fmaf(4.f, po, 2.f * pe);
+}
+
+// G = 2: meshes up to 256 rows, n/8 lanes per row, two rows per pass;
+// G = 4: 512-row meshes, 32 lanes (one warp) per row, one row per pass
+template <int G, int NT>
+__global__ void __launch_bounds__(NT, G == 2 ? 4 : 2)
 k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          uint32_t ntiles, const float* __restrict__ tabs,
          const float* __restrict__ dwt, const RowInfo* __restrict__ rinfo,
@@ -1485,7 +1616,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     {
         float4* r4 = reinterpret_cast<float4*>(ring);
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int i = threadIdx.x; i < rb * rs / 4; i += RTHREADS) {
+        for (int i = threadIdx.x; i < rb * rs / 4; i += NT) {
             r4[i] = z;
         }
     }
@@ -1532,10 +1663,10 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         const int n = int(B.n);
         const int x0 = int(t.x0);
         const int rows = int(t.rows);
-        const int seg = n >> 3;
+        const int seg = n / (4 * G);   // lanes per row
         const int l = threadIdx.x % seg;
         const int rl = threadIdx.x / seg;
-        const int rp = RTHREADS / seg;
+        const int rp = NT / seg;
         const int as = astride0(n);
 
         // stage 1: both y-kicks of the new rows, in place
@@ -1557,18 +1688,26 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 for (int j = l; j < 12; j += seg) {
                     reinterpret_cast<float4*>(row + APAD + n)[j] = z;
                 }
+                const int gw = n / G;   // columns per lane group
                 if (unsigned(x) < unsigned(n)) {
                     const RowInfo ri = S[i];
                     __syncwarp(rmask);
-                    const int ya = 4 * l, yb = (n >> 1) + 4 * l;
-                    const float4 oa = ykick4(row, as, n, ya, ri);
-                    const float4 ob = ykick4(row, as, n, yb, ri);
+                    float4 o[G];
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        o[g] = ykick4(row, as, n, g * gw + 4 * l, ri);
+                    }
                     __syncwarp(rmask);
-                    *reinterpret_cast<float4*>(row + APAD + ya) = oa;
-                    *reinterpret_cast<float4*>(row + APAD + yb) = ob;
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        *reinterpret_cast<float4*>(row + APAD + g * gw
+                                                   + 4 * l) = o[g];
+                    }
                 } else {
-                    reinterpret_cast<float4*>(row + APAD)[l] = z;
-                    reinterpret_cast<float4*>(row + APAD + (n >> 1))[l] = z;
+#pragma unroll
+                    for (int g = 0; g < G; g++) {
+                        reinterpret_cast<float4*>(row + APAD + g * gw)[l] = z;
+                    }
                 }
             }
         }
@@ -1600,7 +1739,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
 
         // drift x-kick, Fokker-Planck, output rows and projections, two
         // rows per lane segment
-        {
+        if constexpr (G == 2) {
             const float* W = dwt + B.dw_off;      // drift planes [5][n]
             const float* F = W + 5 * n;           // Fokker-Planck [5][n]
             const float h03 = tabs[B.tab_off + TAB_WS * n];
@@ -1626,6 +1765,31 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 }
                 if ((l & (hw - 1)) == 0 && (up ? v1 : v0)) {
                     pout[B.prof_off + X0 + (up ? 1 : 0)] = h03 * v;
+                }
+            }
+        } else {
+            // one row per warp and pass, G groups of 4 columns per lane
+            const float* W = dwt + B.dw_off;      // drift planes [5][n]
+            const float* F = W + 5 * n;           // Fokker-Planck [5][n]
+            const float h03 = tabs[B.tab_off + TAB_WS * n];
+            const int gw = n / G;
+            for (int rbase = 0; rbase < rows; rbase += rp) {
+                const int r = rbase + rl;
+                const bool valid = r < rows;
+                const int X = x0 + (valid ? r : 0);
+                float d[G][4];
+#pragma unroll
+                for (int g = 0; g < G; g++) {
+                    drift1(ring, mc, rb, rs, X, g * gw + 4 * l, W, n, d[g]);
+                }
+                float* o = dout + B.dens_off + size_t(X) * n;
+                float v = fp_row<G>(d, l, n, F, o, valid);
+#pragma unroll
+                for (int q = 16; q > 0; q >>= 1) {
+                    v += __shfl_xor_sync(0xffffffffu, v, q);
+                }
+                if (l == 0 && valid) {
+                    pout[B.prof_off + X] = h03 * v;
                 }
             }
         }
