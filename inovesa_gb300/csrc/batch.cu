@@ -53,8 +53,7 @@ struct vfps_batch {
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
     // tile lists: TL_RING (chain 0, n <= 256), TL_RING4 (chain 0, n = 512),
-    // TL_ROT (chain 1), TL_WIDE
-    // (chain 0, n >= 512)
+    // TL_ROT (chain 1), TL_WIDE (chain 0, n >= 1024)
     std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
     uint32_t max_n = 0;
