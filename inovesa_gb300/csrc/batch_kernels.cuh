@@ -1279,14 +1279,18 @@ __device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
                                            RowInfo* S, uint64_t* bar)
 {
     const int n = int(B.n);
-    const int a = max(lo, 0), e = min(hi, n);
+    // the rows inside the mesh; none when a short last tile's new rows lie
+    // all beyond the mesh end (the previous tile's halo reached past it)
+    const int a = max(lo, 0), e = max(min(hi, n), a);
     const uint32_t row_bytes = uint32_t(n) * 4u;
     const uint32_t ri_bytes = uint32_t(e - a) * uint32_t(sizeof(RowInfo));
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         fence_proxy_async();
         mbar_arrive_expect_tx(bar, uint32_t(e - a) * row_bytes + ri_bytes);
-        tma_load_1d(S + (a - lo), rinfo + B.prof_off + a, ri_bytes, bar);
+        if (e > a) {
+            tma_load_1d(S + (a - lo), rinfo + B.prof_off + a, ri_bytes, bar);
+        }
     }
     __syncwarp();
     for (int x = a + lane; x < e; x += 32) {

@@ -170,6 +170,39 @@ def test_batch_tilings_agree(gpu_ctx, monkeypatch):
         assert rel_l1(got, ref.density(0)) <= TOL, i
 
 
+@pytest.mark.parametrize("n, cells, nb", [(512, "3072", 12),
+                                           (256, "1280", 24)])
+def test_short_tail_tile_beyond_halo(gpu_ctx, monkeypatch, n, cells, nb):
+    """A bunch's last tile shorter than the halo below it (512 rows in
+    6-row tiles end in 2 rows, 256 in 5-row tiles in 1; the linear
+    interpolation's halo is 3 rows deep): when that tile continues its
+    predecessor in one CTA, all of its new staged rows lie beyond the mesh
+    end, and the step must stage none of them.  Enough bunches that the
+    persistent CTAs walk several tiles each; two of them against the
+    oracle."""
+    p0 = P.derive(GridSize=n, StepsPerTs=2000, padding=2.0,
+                  VacuumGap=0.0318)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p0))
+    specs = []
+    for k in range(nb):
+        p = P.derive(GridSize=n, StepsPerTs=2000, padding=2.0,
+                     VacuumGap=0.0318, S_csr=0.2 + 1.2 * k / (nb - 1))
+        specs.append((p, 0, p["Ib"], 2, False))
+    monkeypatch.setenv("VFPS_TILE_CELLS", cells)
+    b = make_batch(gpu_ctx, specs, {n: z})
+    steps = 12
+    b.step(steps)
+    assert gpu_ctx.device_status() == 0
+    dens = b.download()
+    for i in (0, nb - 1):
+        p, ch, ib, it, cl = specs[i]
+        ref = oracle_sim(p, ch, ib, z.data(), it=it, clamp=cl)
+        ref.step(steps)
+        off, _ = b.layout(i)
+        got = dens[off:off + n * n].reshape(n, n)
+        assert rel_l1(got, ref.density(0)) <= TOL, i
+
+
 def test_batch_wide_meshes(gpu_ctx):
     """Meshes of 512 and 1024 rows (the wide chain-0 kernel) next to
     narrow ones (the ring kernel) in one batch, against the FP64 oracle."""
