@@ -9,11 +9,11 @@
 //            impedance in FP64), the charge integral (compensated FP32),
 //            the renormalisation factor of this step, the y-kick stencils
 //            of chain-0 rows and a step ticket.
-//  k_bmaps0  chain 0 (main.cpp's loop) for meshes up to 1024 rows
-//            (template: 2, 4 or 8 column groups per lane): a
+//  k_bmaps0  chain 0 (main.cpp's loop) for meshes up to 256 rows and for
+//            512-row meshes (template: 2 or 4 column groups per lane): a
 //            persistent kernel streaming rows through a ring in shared
 //            memory (launched as a programmatic dependent of k_bwake).
-//  k_bmaps0w  chain 0 for 2048-row meshes on a tile of TX mesh rows: wake
+//  k_bmaps0w  chain 0 for 1024-row meshes on a tile of TX mesh rows: wake
 //            y-kick and RF y-kick fused in registers, drift x-kick,
 //            Fokker-Planck, the new rows and their projections.
 //  k_bmaps1  chain 1 (rotation, wake y-kick, Fokker-Planck).
@@ -41,13 +41,10 @@
 using vfps::DevBuf;
 
 // ================================================================== host
-enum { TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_RING8 = 4,
-       TL_COUNT = 5 };
+enum { TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_COUNT = 4 };
 constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel, G = 2
 constexpr int RING4_N = 512;      // the mesh of the ring kernel, G = 4
 constexpr int RTHREADS4 = 256;    // its CTA: 8 warps, one row each
-constexpr int RING8_N = 1024;     // the mesh of the ring kernel, G = 8
-constexpr int RTHREADS8 = 512;    // its CTA: 16 warps, one row each
 
 struct vfps_batch {
     vfps_ctx* ctx = nullptr;
@@ -55,8 +52,8 @@ struct vfps_batch {
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    // tile lists: TL_RING (chain 0, n <= 256), TL_RING4 / TL_RING8 (chain
-    // 0, n = 512 / 1024), TL_ROT (chain 1), TL_WIDE (chain 0, n = 2048)
+    // tile lists: TL_RING (chain 0, n <= 256), TL_RING4 (chain 0, n = 512),
+    // TL_ROT (chain 1), TL_WIDE (chain 0, n = 1024)
     std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
     uint32_t max_n = 0;
@@ -80,8 +77,6 @@ struct vfps_batch {
     unsigned gridR = 0;        // persistent CTAs of k_bmaps0
     SmemR layoutR4{};          // the same for the 512-row ring kernel
     unsigned gridR4 = 0;
-    SmemR layoutR8{};          // and for the 1024-row ring kernel
-    unsigned gridR8 = 0;
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
@@ -238,8 +233,6 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
                 b->layoutR);
     ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
                 b->layoutR4);
-    ring_launch(k_bmaps0<8, RTHREADS8>, TL_RING8, b->gridR8, RTHREADS8,
-                b->layoutR8);
     if (!b->htiles[TL_WIDE].empty()) {
         k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], st>>>(
             b->bd.p, b->tiles[TL_WIDE].p,
@@ -289,17 +282,16 @@ void build_tiles(vfps_batch* b, int tile_cells)
     int max_rows = 0;
     // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
-    int ring_rows = 0, ring_n = 0, ring4_rows = 0, ring8_rows = 0;
+    int ring_rows = 0, ring_n = 0, ring4_rows = 0;
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
         const int c = B.chain == 1 ? TL_ROT
-                      : n <= RING_MAX_N ? TL_RING
-                      : n == RING4_N ? TL_RING4
-                      : n == RING8_N ? TL_RING8
-                                     : TL_WIDE;
+                      : (n <= RING_MAX_N ? TL_RING
+                                         : (n == RING4_N ? TL_RING4
+                                                         : TL_WIDE));
         int tx = std::max(4, tile_cells / n);
-        if (c == TL_RING || c == TL_RING4 || c == TL_RING8) {
+        if (c == TL_RING || c == TL_RING4) {
             // the ring holds two tiles with their halos: at most 32 staged
             // rows per tile keeps it at 64 slots
             tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
@@ -316,8 +308,6 @@ void build_tiles(vfps_batch* b, int tile_cells)
             ring_n = std::max(ring_n, n);
         } else if (c == TL_RING4) {
             ring4_rows = std::max(ring4_rows, nr);
-        } else if (c == TL_RING8) {
-            ring8_rows = std::max(ring8_rows, nr);
         } else if (c == TL_WIDE) {
             a_floats = std::max(a_floats, size_t(nr) * astride0(n));
             b_floats = std::max(b_floats, size_t(nr) * n);
@@ -360,12 +350,6 @@ void build_tiles(vfps_batch* b, int tile_cells)
         b->gridR4 = persistent_grid(b, k_bmaps0<4, RTHREADS4>, RTHREADS4,
                                     b->smem[TL_RING4],
                                     b->htiles[TL_RING4].size());
-    }
-    if (!b->htiles[TL_RING8].empty()) {
-        b->smem[TL_RING8] = ring_layout(b->layoutR8, ring8_rows, RING8_N);
-        b->gridR8 = persistent_grid(b, k_bmaps0<8, RTHREADS8>, RTHREADS8,
-                                    b->smem[TL_RING8],
-                                    b->htiles[TL_RING8].size());
     }
     if (!b->htiles[TL_WIDE].empty()) {
         Smem0& L = b->layout0;
@@ -410,10 +394,6 @@ void upload_tiles(vfps_batch* b)
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
                                        b->smem[TL_RING4], 1))));
-    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<8, RTHREADS8>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   static_cast<int>(std::max<size_t>(
-                                       b->smem[TL_RING8], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0w,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
@@ -715,8 +695,9 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         for (uint32_t i = 0; i < nb; i++) {
             const vfps_bunch_desc& d = desc[i];
             const uint32_t n = d.n;
-            VFPS_REQUIRE(n >= 64 && n <= 2048 && (n & (n - 1)) == 0,
-                         "batched meshes must be a power of two, 64..2048");
+            VFPS_REQUIRE(n >= 64 && n <= 1024 && (n & (n - 1)) == 0,
+                         "batched meshes must be a power of two, 64..1024 "
+                         "(wider meshes run on the plain path)");
             VFPS_REQUIRE(d.it >= 2 && d.it <= 4,
                          "batched interpolation points must be 2..4");
             VFPS_REQUIRE(d.chain == 0 || d.chain == 1, "chain must be 0 or 1");

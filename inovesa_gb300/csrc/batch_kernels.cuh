@@ -1599,10 +1599,9 @@ __device__ __forceinline__ float fp_row(const float (&d)[G][4], int l, int n,
 }
 
 // G = 2: meshes up to 256 rows, n/8 lanes per row, two rows per pass;
-// G = 4, 8: 512- and 1024-row meshes, 32 lanes (one warp) per row, one row
-// per pass
+// G = 4: 512-row meshes, 32 lanes (one warp) per row, one row per pass
 template <int G, int NT>
-__global__ void __launch_bounds__(NT, G == 2 ? 4 : (G == 4 ? 2 : 1))
+__global__ void __launch_bounds__(NT, G == 2 ? 4 : 2)
 k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          uint32_t ntiles, const float* __restrict__ tabs,
          const float* __restrict__ dwt, const RowInfo* __restrict__ rinfo,

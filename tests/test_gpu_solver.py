@@ -203,9 +203,21 @@ def test_short_tail_tile_beyond_halo(gpu_ctx, monkeypatch, n, cells, nb):
         assert rel_l1(got, ref.density(0)) <= TOL, i
 
 
+def test_batch_rejects_wider_meshes(gpu_ctx):
+    """Batched meshes go up to 1024 rows (the ring kernel); a 2048-row mesh
+    is refused with a clear error (the plain path takes it)."""
+    p = P.derive(GridSize=2048, StepsPerTs=4000, padding=2.0,
+                 VacuumGap=0.0318, S_csr=0.6)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    with pytest.raises(V.InvalidArgument, match="64..1024"):
+        make_batch(gpu_ctx, [(p, 0, p["Ib"], 4, False)], {2048: z})
+    assert gpu_ctx.device_status() == 0
+
+
 def test_batch_wide_meshes(gpu_ctx):
-    """Meshes of 512 and 1024 rows (the wide chain-0 kernel) next to
-    narrow ones (the ring kernel) in one batch, against the FP64 oracle."""
+    """Meshes of 512 rows (the ring kernel with four column groups per
+    lane) and 1024 rows (the tiled chain-0 kernel) next to narrow ones in
+    one batch, against the FP64 oracle."""
     specs, z_by_n, zdata = [], {}, {}
     for n in (128, 512, 1024):
         spt = 1000 if n < 1024 else 2000
