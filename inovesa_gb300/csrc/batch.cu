@@ -200,9 +200,10 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     VFPS_LAUNCHED();
     mark(1);
     // programmatic dependent launch of the first ring kernel: its CTAs zero
-    // their rings and set up their barriers while k_bwake runs, then wait
-    // for it to finish (griddepcontrol.wait) before they read or write
-    // device memory.  Only ring kernels are launched so: k_bwake CTAs
+    // their rings, set up their barriers and start the bulk copies of their
+    // first density rows while k_bwake runs, then wait for it to finish
+    // (griddepcontrol.wait) before they read its stencils or write device
+    // memory.  Only ring kernels are launched so: k_bwake CTAs
     // launched early crowd onto the SMs that finish first, which is slower.
     cudaLaunchAttribute pdl[1];
     pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;

@@ -1269,14 +1269,18 @@ struct RingMap {
 };
 
 // bulk copies of the mesh rows among [lo, hi) into their slots, and of
-// their y-kick stencils into S[x - lo] (warp 0; lane 0 arms the barrier
-// with the byte count first)
+// their y-kick stencils into S[x - lo] (warp 0).  The rows part arms the
+// barrier with the byte count of both parts first (lane 0); the stencils
+// part may follow later, the barrier's phase completes when both have
+// landed.
 __device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
                                            const RingMap& m, float* ring,
                                            int rb, int rs,
                                            const float* __restrict__ din,
                                            const RowInfo* __restrict__ rinfo,
-                                           RowInfo* S, uint64_t* bar)
+                                           RowInfo* S, uint64_t* bar,
+                                           bool rows = true,
+                                           bool stencils = true)
 {
     const int n = int(B.n);
     // the rows inside the mesh; none when a short last tile's new rows lie
@@ -1286,16 +1290,21 @@ __device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
     const uint32_t ri_bytes = uint32_t(e - a) * uint32_t(sizeof(RowInfo));
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
-        fence_proxy_async();
-        mbar_arrive_expect_tx(bar, uint32_t(e - a) * row_bytes + ri_bytes);
-        if (e > a) {
+        if (rows) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(bar,
+                                  uint32_t(e - a) * row_bytes + ri_bytes);
+        }
+        if (stencils && e > a) {
             tma_load_1d(S + (a - lo), rinfo + B.prof_off + a, ri_bytes, bar);
         }
     }
-    __syncwarp();
-    for (int x = a + lane; x < e; x += 32) {
-        tma_load_1d(ring + size_t(m.slot(x, rb)) * rs + APAD,
-                    din + B.dens_off + size_t(x) * n, row_bytes, bar);
+    if (rows) {
+        __syncwarp();
+        for (int x = a + lane; x < e; x += 32) {
+            tma_load_1d(ring + size_t(m.slot(x, rb)) * rs + APAD,
+                        din + B.dens_off + size_t(x) * n, row_bytes, bar);
+        }
     }
 }
 
@@ -1630,8 +1639,6 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         mbar_fence_init();
     }
     fence_proxy_async();
-    // this step's stencils and the previous step's density are complete
-    pdl_wait();
     __syncthreads();
 
     // each CTA walks a contiguous chunk of the tile list: tiles of a bunch
@@ -1655,10 +1662,20 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         hi_c = int(t.x0 + t.rows) + B.halo_hi;
         mc = RingMap{lo_c, 0};
         front = hi_c - lo_c;
+        // the first tile's density rows already while the stencil kernel
+        // runs: the previous step wrote them and had completed before that
+        // kernel started
         if (warp == 0) {
             issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, rinfo, S,
-                       &bar[0]);
+                       &bar[0], true, false);
         }
+    }
+    // this step's stencils are complete
+    pdl_wait();
+    if (t_begin < t_end && warp == 0) {
+        const BDev B = bd[tiles[t_begin].bunch];
+        issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, rinfo, S, &bar[0],
+                   false, true);
     }
     int bad = 0;
     for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
