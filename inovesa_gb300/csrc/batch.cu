@@ -68,7 +68,10 @@ struct vfps_batch {
     DevBuf<float> wake, factor;
     DevBuf<RowInfo> rinfo;     // chain-0 y-kick stencils of every row
     DevBuf<double> filling;
-    // step tickets: every k_bwake CTA takes one, so step = tickets / nb
+    // k_bwake's CTAs: (bunch, first row) of each block of rows
+    DevBuf<uint2> wblk;
+    uint32_t nwblk = 0;
+    // step tickets: every k_bwake CTA takes one, so step = tickets / nwblk
     DevBuf<unsigned long long> tickets;
     int cur = 0;               // buffer holding the current state
     size_t smem[TL_COUNT] = {};
@@ -190,12 +193,12 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             b->wake.p, b->ctx->d_status);
         VFPS_LAUNCHED();
     }
-    k_bwake<<<b->nb, THREADS, wsm, st>>>(
-        b->bd.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p, b->wake.p,
-        b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p, b->beams.p,
-        b->members.p,
+    k_bwake<<<b->nwblk, THREADS, wsm, st>>>(
+        b->bd.p, b->wblk.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p,
+        b->wake.p, b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p,
+        b->beams.p, b->members.p,
         CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
-               b->csr_every, b->csr_cap},
+               b->csr_every, b->csr_cap, b->nb},
         b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
@@ -911,6 +914,20 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             }
         };
         put(b->bd, b->hb);
+        {
+            // k_bwake: one CTA per block of rows
+            std::vector<uint2> wblk;
+            for (uint32_t i = 0; i < nb; i++) {
+                const uint32_t n = b->hb[i].n;
+                const uint32_t R = static_cast<uint32_t>(
+                    wake_block_rows(static_cast<int>(n)));
+                for (uint32_t x0 = 0; x0 < n; x0 += R) {
+                    wblk.push_back(make_uint2(i, x0));
+                }
+            }
+            b->nwblk = static_cast<uint32_t>(wblk.size());
+            put(b->wblk, wblk);
+        }
         put(b->tabs, tabs);
         put(b->st, sts);
         put(b->fp5, fp5);

@@ -62,6 +62,7 @@ struct CsrRec {
     unsigned long long* steps;   // ring [cap]: the step in each slot
     uint32_t every;              // record steps with step % every == 0
     uint32_t cap;                // (every == 0: no recording)
+    uint32_t nb;                 // bunches (the power ring's row length)
 };
 
 // the beam of a bunch: bunches of one beam share a padded profile (their
@@ -107,6 +108,15 @@ using namespace vfps::dev;
 __host__ __device__ inline size_t align16(size_t v)
 {
     return (v + 15) & ~size_t(15);
+}
+
+// rows of a k_bwake block of an n-row mesh: meshes up to 256 rows are one
+// block, wider ones blocks of 128 rows (a block's wake sum costs its rows
+// times n; measured, one block beats two for 256 rows and four blocks beat
+// two for 512)
+__host__ __device__ inline int wake_block_rows(int n)
+{
+    return n <= 256 ? n : 128;
 }
 
 // staged row of chain 0: APAD zeros, the n mesh values, APAD + 16 zeros
@@ -169,19 +179,21 @@ __device__ __forceinline__ FF ff_add(FF a, FF b)
     return FF{hi, __fsub_rn(e, __fsub_rn(hi, s))};
 }
 
-// Toeplitz sum wake[x] = sum_m w[x - m] P[m] of a CTA of THREADS threads,
-// from W[k + k/8] = w[k - (n-1)] (one pad entry per 8 puts the lanes below
-// on 32 banks).  Thread = (group g of 8 consecutive rows, slice q of the m
-// range); the 8 rows read W at consecutive places, so stepping m slides a
-// register window by one: 2 shared loads (P broadcast, W) per 8
-// multiply-adds, the same trip count in every lane.  Writes the partial
-// sums partial[q][x] (Q = THREADS / (n/8) slices; n a power of two,
-// 64..2048); the caller sums them after a barrier.
+// Toeplitz sum wake[x] = sum_m w[x - m] P[m] over rows x0 <= x < x0 + R
+// of a CTA of THREADS threads, from W[k + k/8] = w[x0 + k - (n-1)] (one pad
+// entry per 8 puts the lanes below on 32 banks).  Thread = (group g of 8
+// consecutive rows, slice q of the m range); the 8 rows read W at
+// consecutive places, so stepping m slides a register window by one: 2
+// shared loads (P broadcast, W) per 8 multiply-adds, the same trip count in
+// every lane.  Writes the partial sums partial[q][x - x0] (Q = THREADS /
+// (R/8) slices; n and R powers of two, 64 <= R <= n <= 2048, R <= 8
+// THREADS); the caller sums them after a barrier.
 __device__ __forceinline__ void toeplitz_partials(const float* P,
                                                   const float* W,
-                                                  float* partial, int n)
+                                                  float* partial, int n,
+                                                  int R)
 {
-    const int G = n >> 3;                    // <= THREADS
+    const int G = R >> 3;                    // <= THREADS
     const int Q = THREADS / G;
     const int q = threadIdx.x / G;
     const int g = threadIdx.x % G;
@@ -214,33 +226,38 @@ __device__ __forceinline__ void toeplitz_partials(const float* P,
     // two 16-byte stores (partial starts 16-byte aligned: 13n bytes into
     // the shared memory for n >= 64): a stride of 8 floats between lanes
     // costs 8 wavefronts per store instead of 8 scalar 8-way conflicts
-    float4* pr = reinterpret_cast<float4*>(partial + size_t(q) * n + x);
+    float4* pr = reinterpret_cast<float4*>(partial + size_t(q) * R + x);
     pr[0] = make_float4(acc[0], acc[1], acc[2], acc[3]);
     pr[1] = make_float4(acc[4], acc[5], acc[6], acc[7]);
 }
 
-// W[k + k/8] = w[(delta + k - (n-1)) mod nmax] for k < 2n - 1 (the layout
-// that toeplitz_partials reads): the field at distance delta + x - m of a
-// source cell m on row x (delta: the distance between two bunches' buckets
-// in the padded profile, 0 for a bunch's own field)
+// W[k + k/8] = w[(delta + k - (n-1)) mod nmax] for k < R + n - 1 (the
+// layout that toeplitz_partials reads for R rows): the field at distance
+// delta + x - m of a source cell m on row x (delta: the first row of the
+// block plus the distance between two bunches' buckets in the padded
+// profile, 0 for the rows of a bunch's own field from row 0)
 __device__ __forceinline__ void load_toeplitz(const float* __restrict__ w,
                                               int nmax, int n, float* W,
-                                              long long delta = 0)
+                                              long long delta, int R)
 {
-    for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
+    for (int k = threadIdx.x; k < R + n - 1; k += THREADS) {
         long long d = (delta + k - (n - 1)) % nmax;
         d += d < 0 ? nmax : 0;
         W[k + (k >> 3)] = w[d];
     }
 }
 
-// One CTA per bunch: wake potential of the previous step's profile, charge
-// integral, renormalisation factor and, for chain 0, both y-kick stencils
-// of every row.  The step number comes from a 64-bit ticket that every CTA
-// takes once per step (nb tickets per step), so no CTA has to wait for the
-// others or reset anything.
+// One CTA per block of rows of a bunch (wake_block_rows; wblk: bunch and
+// first row of each CTA): wake potential of the previous step's profile on
+// the block's rows, charge integral, renormalisation factor and, for chain 0,
+// both y-kick stencils of the block's rows.  Every CTA of a bunch sums the
+// whole profile's charge (the same bits); the first one stores it.  The
+// step number comes from a 64-bit ticket that every CTA takes once per
+// step (one ticket per CTA and step), so no CTA has to wait for the others
+// or reset anything.
 __global__ void __launch_bounds__(THREADS)
-k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
+k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
+        const float* __restrict__ tabs,
         const float* __restrict__ wt, const RowStencil* __restrict__ st,
         const float* __restrict__ pin, float* __restrict__ wake,
         RowInfo* __restrict__ rinfo, float* __restrict__ factor,
@@ -255,9 +272,12 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     __shared__ unsigned long long ticket_s;
     // the maps kernel that follows may start its prologue now
     pdl_trigger();
-    const uint32_t b = blockIdx.x;
+    const uint2 blk = wblk[blockIdx.x];
+    const uint32_t b = blk.x;
     const BDev B = bd[b];
     const int n = int(B.n);
+    const int xr0 = int(blk.y);                   // first row of the block
+    const int R = wake_block_rows(n);             // rows of the block
     // W[k + k/8] = w[(k - (n-1)) mod nmax] for k < 2n - 1: one pad entry
     // per 8 puts the 32 lanes of the wake sum (rows 8 apart) on 32 banks
     float* W = P + n;
@@ -273,7 +293,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     // the bunch's own field (a coupled beam reloads it per member; not
     // waiting for the beam record keeps this load off its latency)
     if (sum_here) {
-        load_toeplitz(wt + B.wt_off, int(B.nmax), n, W);
+        load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, xr0, R);
     }
     const BeamDev Mb = beams[b];
     const bool coupled = Mb.count > 1;
@@ -283,8 +303,8 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     const float ws0 = x0 < n ? ws[x0] : 0.f;
     const RowStencil* rf = st + B.st_off + ST_RF * n;
     RowStencil sb0 = {};
-    if (B.chain == 0 && x0 < n) {
-        sb0 = rf[x0];
+    if (B.chain == 0 && x0 < R) {
+        sb0 = rf[xr0 + x0];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -306,16 +326,16 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             red[warp] = make_float2(a.hi, a.lo);
         }
     }
-    float* partial = W + 2 * n + (n >> 2);   // [Q][n], Q n = 8 THREADS
-    const int Q = THREADS / (n >> 3);
-    float* acc = partial + 8 * THREADS;      // coupled beams: wake [n]
+    float* partial = W + 2 * n + (n >> 2);   // [Q][R], Q R = 8 THREADS
+    const int Q = THREADS / (R >> 3);
+    float* acc = partial + 8 * THREADS;      // coupled beams: wake [R]
     float* Pm = acc + n;                     // and a member's profile [n]
     if (sum_here && !coupled) {
-        toeplitz_partials(P, W, partial, n);
+        toeplitz_partials(P, W, partial, n, R);
     } else if (sum_here) {
         // the fields of every member of the beam (this bunch included) at
         // their bucket distances
-        for (int x = threadIdx.x; x < n; x += THREADS) {
+        for (int x = threadIdx.x; x < R; x += THREADS) {
             acc[x] = 0.f;
         }
         for (uint32_t k = 0; k < Mb.count; k++) {
@@ -327,14 +347,14 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             for (int i = threadIdx.x; i < n; i += THREADS) {
                 Pm[i] = pin[B2.prof_off + i];
             }
-            load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, delta);
+            load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, delta + xr0, R);
             __syncthreads();
-            toeplitz_partials(Pm, W, partial, n);
+            toeplitz_partials(Pm, W, partial, n, R);
             __syncthreads();
-            for (int x = threadIdx.x; x < n; x += THREADS) {
+            for (int x = threadIdx.x; x < R; x += THREADS) {
                 float sum = 0.f;
                 for (int q = 0; q < Q; q++) {
-                    sum += partial[size_t(q) * n + x];
+                    sum += partial[size_t(q) * R + x];
                 }
                 acc[x] += sum;   // read back by this thread only
             }
@@ -361,7 +381,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     } else if (renorm_now) {
         fac = 0.f;
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && xr0 == 0) {
         filling[b] = double(tot.hi) + double(tot.lo);
         factor[b] = fac;
         if (B.fillset > 0 && !(tot.hi > 0.f)) {
@@ -372,15 +392,16 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
     // of the row for this step, the renormalisation factor folded into the
     // first (both kicks are linear)
     const bool chain0 = B.chain == 0;
-    for (int x = threadIdx.x; x < n; x += THREADS) {
+    for (int xl = threadIdx.x; xl < R; xl += THREADS) {
+        const int x = xr0 + xl;
         float v = 0.f;
         if (sum_here) {
             float sum = 0.f;
             if (coupled) {
-                sum = acc[x];
+                sum = acc[xl];
             } else {
                 for (int k = 0; k < Q; k++) {
-                    sum += partial[size_t(k) * n + x];
+                    sum += partial[size_t(k) * R + xl];
                 }
             }
             v = __fmul_rn(B.wakescale, sum);
@@ -401,7 +422,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             sa.w[0] = 1.f;
             sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
         }
-        const RowStencil sb = x == x0 ? sb0 : rf[x];
+        const RowStencil sb = xl == x0 ? sb0 : rf[x];
         RowInfo ri;
         ri.s = sa.shift0 + sb.shift0;
         ri.sb = sb.shift0;
@@ -414,8 +435,8 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         rinfo[B.prof_off + x] = ri;
     }
     // CSR power of this step's profile (recording steps only; the same
-    // decision in every CTA)
-    if (csr.every == 0 || step % csr.every != 0) {
+    // decision in every CTA; the bunch's first CTA)
+    if (csr.every == 0 || step % csr.every != 0 || xr0 != 0) {
         return;
     }
     const uint32_t koff = csr.off[b];
@@ -427,12 +448,13 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
         W[k + (k >> 3)] = csr.k[koff + k];
     }
     __syncthreads();
-    toeplitz_partials(P, W, partial, n);
+    toeplitz_partials(P, W, partial, n, n);
     __syncthreads();
+    const int Qn = THREADS / (n >> 3);
     FF dot = FF{0.f, 0.f};
     for (int x = threadIdx.x; x < n; x += THREADS) {
         float v = 0.f;
-        for (int q = 0; q < Q; q++) {
+        for (int q = 0; q < Qn; q++) {
             v += partial[size_t(q) * n + x];
         }
         dot = ff_add(dot, ff_prod(P[x], v));
@@ -454,7 +476,7 @@ k_bwake(const BDev* __restrict__ bd, const float* __restrict__ tabs,
             tot = ff_add(tot, FF{red[w2].x, red[w2].y});
         }
         const uint32_t slot = (step / csr.every) % csr.cap;
-        csr.power[size_t(slot) * gridDim.x + b] = tot.hi + tot.lo;
+        csr.power[size_t(slot) * csr.nb + b] = tot.hi + tot.lo;
         if (b == 0) {
             csr.steps[slot] = step;
         }
@@ -630,7 +652,7 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
     }
     const bool has_wake = B.flags & F_WAKE;
     if (has_wake) {
-        load_toeplitz(wt + B.wt_off, int(B.nmax), n, W);
+        load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, 0, n);
     }
     __syncthreads();
     block_trapezoid(D, G, n, scratch);
@@ -654,7 +676,7 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
     for (int it = 0; it <= last; it++) {
         // row kicks of the current profile (the first pass: RF only)
         if (has_wake && it > 0) {
-            toeplitz_partials(P, W, partial, n);
+            toeplitz_partials(P, W, partial, n, n);
         }
         __syncthreads();
         for (int x = threadIdx.x; x < n; x += THREADS) {

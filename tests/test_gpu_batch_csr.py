@@ -15,9 +15,10 @@ from inovesa_gb300 import vfps as V
 
 pytestmark = pytest.mark.gpu
 
-# (mesh, S, gap): shielded and free-space CSR, two mesh sizes
+# (mesh, S, gap): shielded and free-space CSR, three mesh sizes (the
+# 512-row mesh's wake is summed in blocks by several CTAs)
 CASES = [(256, 0.3, 0.0318), (256, 1.0, 0.0318), (128, 0.5, -1.0),
-         (256, 0.1, -1.0)]
+         (256, 0.1, -1.0), (512, 0.6, 0.0318)]
 
 
 def build(ctx, spt=500):
@@ -59,17 +60,17 @@ def test_csr_every_and_ring(gpu_ctx):
     b, ps, zc = build(gpu_ctx)
     nb = len(CASES)
     # bunch 1 without CSR; record every third step into 3 slots
-    b.set_csr(zc, [0, -1, 2, 3], [p["fc"] for p in ps],
+    b.set_csr(zc, [0, -1, 2, 3, 4], [p["fc"] for p in ps],
               [P.C / p["bl"] for p in ps], every=3, capacity=3)
     b.step(14)
     steps, power = b.csr()
     assert steps.tolist() == [6, 9, 12]
-    assert np.all(power[:, 1] == 0) and np.all(power[:, [0, 2, 3]] > 0)
+    assert np.all(power[:, 1] == 0) and np.all(power[:, [0, 2, 3, 4]] > 0)
     b.step(1)     # step 14: not recorded
     steps2, _ = b.csr()
     assert steps2.tolist() == [6, 9, 12]
     # step 15 against the plain ElectricField of the state it starts from
-    b.set_csr(zc, [0, 1, 2, 3], [p["fc"] for p in ps],
+    b.set_csr(zc, [0, 1, 2, 3, 4], [p["fc"] for p in ps],
               [P.C / p["bl"] for p in ps], every=1, capacity=2)
     n, p = CASES[0][0], ps[0]
     d = b.density(0).copy()

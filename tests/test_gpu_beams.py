@@ -5,7 +5,8 @@ bunch filling src/main.cpp:248-321).
 
 Checks: one step's wake against the oracle's coupled wake of the same
 profiles (1e-5 of the largest |wake|, the FP32 Toeplitz sum against the
-FFT); 40 steps of a three-bunch beam against the plain one-map-per-launch
+FFT), on 64-row meshes and on 512-row meshes (rows summed in blocks by
+several CTAs per bunch); 40 steps of a three-bunch beam against the plain one-map-per-launch
 loop over a three-bunch phase space (density L1 <= 1e-4, the metric's bar);
 a bunch outside the beam is unaffected by it; inconsistent beams are
 rejected."""
@@ -43,19 +44,30 @@ def rel_l1(a, b):
                  / np.abs(b).sum())
 
 
-def test_coupled_wake_matches_oracle(gpu_ctx):
-    p, z, b = setup(gpu_ctx)
-    b.set_beams([1, 1, 1, 0], BUCKETS + [0], SPACING, FILL + [1.0])
+# (mesh, padding, bucket spacing): one block of rows per bunch, and 512-row
+# meshes whose wake is summed by several CTAs per bunch
+WAKE_CASES = [(N, 16.0, SPACING), (512, 4.0, 500)]
+
+
+@pytest.mark.parametrize("n, padding, spacing", WAKE_CASES)
+def test_coupled_wake_matches_oracle(gpu_ctx, n, padding, spacing):
+    p = P.derive(GridSize=n, StepsPerTs=SPT, padding=padding,
+                 VacuumGap=0.0318, S_csr=0.5)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"], impedance=0)
+             for _ in range(4)]
+    b = V.BunchBatch(gpu_ctx, descs, [z])
+    b.set_beams([1, 1, 1, 0], BUCKETS + [0], spacing, FILL + [1.0])
     lay = [b.layout(i) for i in range(4)]
     pr = b.profiles()
-    prof = np.stack([pr[lay[i][1]:lay[i][1] + N] for i in range(4)])
+    prof = np.stack([pr[lay[i][1]:lay[i][1] + n] for i in range(4)])
     assert np.allclose(b.filling()[:3], FILL, rtol=1e-5)
     b.step(1)
     wk = b.wake()
-    got = np.stack([wk[lay[i][1]:lay[i][1] + N] for i in range(4)])
+    got = np.stack([wk[lay[i][1]:lay[i][1] + n] for i in range(4)])
     ws = float(np.float32(b.descs[0].wakescaling))
     ref = oracle.wake_potential(prof[:3], z.data(), ws, buckets=BUCKETS,
-                                spacing=SPACING)
+                                spacing=spacing)
     assert np.abs(got[:3] - ref).max() <= 1e-5 * np.abs(ref).max()
     alone = oracle.wake_potential(prof[3:], z.data(), ws)[0]
     assert np.abs(got[3] - alone).max() <= 1e-5 * np.abs(alone).max()
