@@ -94,6 +94,8 @@ struct vfps_batch {
     DevBuf<uint32_t> csroff;   // per bunch: its table or NO_CSR
     DevBuf<float> csrpow;      // ring [cap][nb]
     DevBuf<unsigned long long> csrsteps;   // ring [cap]
+    DevBuf<float2> csrpart;    // [nb][CSR_MAXBLK] blocks' parts of a step
+    DevBuf<unsigned> csrdone;  // [nb] blocks done (reset by the last)
     uint32_t csr_every = 0, csr_cap = 0;
     DevBuf<float> tplanes;
     DevBuf<TcGroup> tcg;
@@ -198,7 +200,7 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
         b->wake.p, b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p,
         b->beams.p, b->members.p,
         CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
-               b->csr_every, b->csr_cap, b->nb},
+               b->csr_every, b->csr_cap, b->nb, b->csrpart.p, b->csrdone.p},
         b->ctx->d_status, tc ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
@@ -950,6 +952,9 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             b->csrk.alloc(1);
             b->csrpow.alloc(1);
             b->csrsteps.alloc(1);
+            b->csrpart.alloc(size_t(nb) * CSR_MAXBLK);
+            b->csrdone.alloc(nb);
+            VFPS_CUDA(cudaMemset(b->csrdone.p, 0, b->csrdone.bytes()));
         }
         b->wt.alloc(std::max<size_t>(wt.size(), 1));
         for (uint32_t k = 0; k < nimp; k++) {

@@ -63,7 +63,11 @@ struct CsrRec {
     uint32_t every;              // record steps with step % every == 0
     uint32_t cap;                // (every == 0: no recording)
     uint32_t nb;                 // bunches (the power ring's row length)
+    float2* part;                // [nb][CSR_MAXBLK]: blocks' sums (hi, lo)
+    unsigned* done;              // [nb]: blocks of the step that are done
 };
+// most k_bwake blocks of one bunch (1024 rows in blocks of 128)
+constexpr int CSR_MAXBLK = 8;
 
 // the beam of a bunch: bunches of one beam share a padded profile (their
 // buckets spacing mesh cells apart, src/PS/ElectricField.cpp:255-263), so
@@ -435,8 +439,10 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
         rinfo[B.prof_off + x] = ri;
     }
     // CSR power of this step's profile (recording steps only; the same
-    // decision in every CTA; the bunch's first CTA)
-    if (csr.every == 0 || step % csr.every != 0 || xr0 != 0) {
+    // decision in every CTA): the block's rows' part of the quadratic form
+    // P^T T_K P; the bunch's last block to finish adds the parts in block
+    // order
+    if (csr.every == 0 || step % csr.every != 0) {
         return;
     }
     const uint32_t koff = csr.off[b];
@@ -444,20 +450,21 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
         return;
     }
     __syncthreads();   // W and the partial sums of the wake are free
-    for (int k = threadIdx.x; k < 2 * n - 1; k += THREADS) {
-        W[k + (k >> 3)] = csr.k[koff + k];
+    // W[k + k/8] = K(xr0 + k - (n-1)) for k < R + n - 1 (the table holds
+    // K(d) for d = 1-n .. n-1)
+    for (int k = threadIdx.x; k < R + n - 1; k += THREADS) {
+        W[k + (k >> 3)] = csr.k[koff + xr0 + k];
     }
     __syncthreads();
-    toeplitz_partials(P, W, partial, n, n);
+    toeplitz_partials(P, W, partial, n, R);
     __syncthreads();
-    const int Qn = THREADS / (n >> 3);
     FF dot = FF{0.f, 0.f};
-    for (int x = threadIdx.x; x < n; x += THREADS) {
+    for (int xl = threadIdx.x; xl < R; xl += THREADS) {
         float v = 0.f;
-        for (int q = 0; q < Qn; q++) {
-            v += partial[size_t(q) * n + x];
+        for (int q = 0; q < Q; q++) {
+            v += partial[size_t(q) * R + xl];
         }
-        dot = ff_add(dot, ff_prod(P[x], v));
+        dot = ff_add(dot, ff_prod(P[xr0 + xl], v));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -475,10 +482,32 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
         for (int w2 = 0; w2 < (THREADS >> 5); w2++) {
             tot = ff_add(tot, FF{red[w2].x, red[w2].y});
         }
-        const uint32_t slot = (step / csr.every) % csr.cap;
-        csr.power[size_t(slot) * csr.nb + b] = tot.hi + tot.lo;
-        if (b == 0) {
-            csr.steps[slot] = step;
+        const int nblk = n / R;
+        bool last = true;
+        if (nblk > 1) {
+            // publish this block's part, then count it (the last block
+            // sees every part: each was written before its count)
+            csr.part[size_t(b) * CSR_MAXBLK + xr0 / R] =
+                make_float2(tot.hi, tot.lo);
+            __threadfence();
+            last = atomicAdd(csr.done + b, 1u) == unsigned(nblk - 1);
+            if (last) {
+                __threadfence();
+                tot = FF{0.f, 0.f};
+                for (int r = 0; r < nblk; r++) {
+                    const float2 v = __ldcg(csr.part
+                                            + size_t(b) * CSR_MAXBLK + r);
+                    tot = ff_add(tot, FF{v.x, v.y});
+                }
+                csr.done[b] = 0u;   // for the next recording step
+            }
+        }
+        if (last) {
+            const uint32_t slot = (step / csr.every) % csr.cap;
+            csr.power[size_t(slot) * csr.nb + b] = tot.hi + tot.lo;
+            if (b == 0) {
+                csr.steps[slot] = step;
+            }
         }
     }
 }
