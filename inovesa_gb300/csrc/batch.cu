@@ -332,10 +332,7 @@ void build_tiles(vfps_batch* b, int tile_cells)
     };
     // the ring holds the staged rows of two tiles with their halos
     auto ring_layout = [&](SmemR& L, int rows, int n) {
-        int rb = 1;
-        while (rb < 2 * rows) {
-            rb *= 2;
-        }
+        const int rb = 2 * rows;
         L.rb = static_cast<uint32_t>(rb);
         L.rs = static_cast<uint32_t>(astride0(n));
         o = 0;

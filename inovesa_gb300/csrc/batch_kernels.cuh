@@ -1218,7 +1218,7 @@ struct SmemR {
     uint32_t ring;  // RB slots of RS floats
     uint32_t s;     // RowInfo of the new rows of one tile
     uint32_t bar;   // two mbarriers
-    uint32_t rb;    // ring slots (power of two)
+    uint32_t rb;    // ring slots: twice the rows a tile reads
     uint32_t rs;    // floats per slot
     uint32_t total;
 };
@@ -1310,12 +1310,21 @@ __device__ __forceinline__ float4 ykick4(const float* row, int as, int n,
     return make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// ring slot of mesh row x of the current segment
+// ring slot of mesh row x: (x - xref + pref) mod rb, where xref is the
+// lowest row the tile reads (its first row less the halo) and pref < rb
+// that row's slot, kept as off = pref - xref; a tile reads fewer than rb
+// rows above xref, so one conditional subtraction reduces the sum (rb need
+// not be a power of two)
 struct RingMap {
-    int xref, pref;
+    int off;
+    __device__ __forceinline__ static RingMap at(int xref, int pref)
+    {
+        return RingMap{pref - xref};
+    }
     __device__ __forceinline__ int slot(int x, int rb) const
     {
-        return (x - xref + pref) & (rb - 1);
+        const int s = x + off;
+        return s >= rb ? s - rb : s;
     }
 };
 
@@ -1703,7 +1712,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
 
     // ring state of the current and of the next tile: slot mapping and the
     // new rows [lo, hi) staged for it
-    RingMap mc{0, 0}, mn{0, 0};
+    RingMap mc{0}, mn{0};
     int lo_c = 0, hi_c = 0, lo_n = 0, hi_n = 0;
     int front = 0;   // ring position after the last staged row
     if (t_begin < t_end) {
@@ -1711,7 +1720,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         const BDev B = bd[t.bunch];
         lo_c = int(t.x0) - B.halo_lo;
         hi_c = int(t.x0 + t.rows) + B.halo_hi;
-        mc = RingMap{lo_c, 0};
+        mc = RingMap::at(lo_c, 0);
         front = hi_c - lo_c;
         // the first tile's density rows already while the stencil kernel
         // runs: the previous step wrote them and had completed before that
@@ -1795,14 +1804,16 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             const bool cont = tn.bunch == t.bunch
                               && int(tn.x0) == x0 + rows;
             hi_n = int(tn.x0 + tn.rows) + Bn.halo_hi;
+            const int xr = int(tn.x0) - Bn.halo_lo;   // lowest row it reads
             if (cont) {
-                mn = mc;
+                // the same slots, referred to the next tile's lowest row
+                mn = RingMap::at(xr, mc.slot(xr, rb));
                 lo_n = hi_c;
             } else {
-                lo_n = int(tn.x0) - Bn.halo_lo;
-                mn = RingMap{lo_n, front};
+                lo_n = xr;
+                mn = RingMap::at(xr, front);
             }
-            front = hi_n - mn.xref + mn.pref;
+            front = mn.slot(hi_n, rb);
             if (warp == 0) {
                 issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo, S,
                            &bar[(k + 1) & 1]);
