@@ -28,7 +28,7 @@ namespace {
 constexpr int THREADS = 256;
 constexpr int ROWPAD = 16;     // extra floats per rotated row (chain 1)
 constexpr int TPAD = 4;        // zero floats on each side of a t3 row
-constexpr int APAD = 32;       // zero floats left of a staged row (chain 0)
+constexpr int APAD = 16;       // zero floats left of a staged row (chain 0)
 constexpr uint64_t WAIT_NS = 1000000000ull;  // bounded TMA waits (1 s)
 
 struct __align__(16) BDev {     // 96 bytes: vector loads of its fields
@@ -1685,7 +1685,8 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     const int rb = int(L.rb), rs = int(L.rs);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    // the ring starts zero: slots are written only in [APAD, APAD + n + 48)
+    // the ring starts zero: slots are written only in
+    // [APAD, n + 2 APAD + 16)
     {
         float4* r4 = reinterpret_cast<float4*>(ring);
         const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -1766,7 +1767,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 float* row = ring + size_t(mc.slot(x, rb)) * rs;
                 // zeros right of the row (the slot may have held a longer
                 // row of another bunch)
-                for (int j = l; j < 12; j += seg) {
+                for (int j = l; j < (APAD + 16) / 4; j += seg) {
                     reinterpret_cast<float4*>(row + APAD + n)[j] = z;
                 }
                 const int gw = n / G;   // columns per lane group
