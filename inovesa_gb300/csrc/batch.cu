@@ -101,6 +101,11 @@ struct vfps_batch {
     DevBuf<TcGroup> tcg;
     DevBuf<uint32_t> tclist;
     uint32_t tc_groups = 0;
+    // a second stream for the maps kernels of the other mesh classes, which
+    // run next to the first ring kernel (fork after k_bwake, join before
+    // the step ends)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};  // 1 step from buffer i
     cudaGraphExec_t graph8[2] = {nullptr, nullptr}; // 8 steps from buffer i
 };
@@ -213,7 +218,26 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     cudaLaunchAttribute pdl[1];
     pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    // the maps kernels of a batch with several mesh classes: the first on
+    // this stream, the others on the side stream, all after k_bwake, so
+    // that each fills the SMs the others leave free (no kernel's tail
+    // idles the GPU); sequential when the kernels are timed one by one
+    int classes = 0;
+    for (int c : {TL_RING, TL_RING4, TL_WIDE, TL_ROT}) {
+        classes += b->htiles[c].empty() ? 0 : 1;
+    }
+    const bool forked = !ev && classes > 1;
+    if (forked) {
+        VFPS_CUDA(cudaEventRecord(b->fork, st));
+        VFPS_CUDA(cudaStreamWaitEvent(b->side, b->fork, 0));
+    }
     bool first_ring = true;
+    bool first = true;   // the next maps kernel is the step's first
+    auto next_stream = [&]() {
+        const cudaStream_t s = first || !forked ? st : b->side;
+        first = false;
+        return s;
+    };
     auto ring_launch = [&](auto kernel, int list, unsigned grid, int threads,
                            const SmemR& layout) {
         if (b->htiles[list].empty()) {
@@ -223,7 +247,7 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
         c.gridDim = dim3(grid);
         c.blockDim = dim3(threads);
         c.dynamicSmemBytes = b->smem[list];
-        c.stream = st;
+        c.stream = next_stream();
         c.attrs = pdl;
         c.numAttrs = first_ring ? 1 : 0;
         first_ring = false;
@@ -240,7 +264,7 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
                 b->layoutR4);
     if (!b->htiles[TL_WIDE].empty()) {
-        k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], st>>>(
+        k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], next_stream()>>>(
             b->bd.p, b->tiles[TL_WIDE].p,
             static_cast<uint32_t>(b->htiles[TL_WIDE].size()), b->tabs.p,
             b->st.p, b->fp5.p, b->rinfo.p, b->dens[from].p,
@@ -250,10 +274,14 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     mark(2);
     if (!b->htiles[TL_ROT].empty()) {
         k_bmaps1<<<static_cast<unsigned>(b->htiles[TL_ROT].size()), THREADS,
-                   b->smem[TL_ROT], st>>>(
+                   b->smem[TL_ROT], next_stream()>>>(
             b->bd.p, b->tiles[TL_ROT].p, b->tabs.p, b->fp5.p, b->wake.p,
             b->factor.p, b->dens[from].p, b->dens[to].p, b->prof[to].p);
         VFPS_LAUNCHED();
+    }
+    if (forked) {
+        VFPS_CUDA(cudaEventRecord(b->join, b->side));
+        VFPS_CUDA(cudaStreamWaitEvent(st, b->join, 0));
     }
     mark(3);
 }
@@ -1040,6 +1068,11 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         b->filling.alloc(nb);
         b->tickets.alloc(1);
         VFPS_CUDA(cudaMemsetAsync(b->tickets.p, 0, b->tickets.bytes(), st));
+        VFPS_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+        VFPS_CUDA(cudaEventCreateWithFlags(&b->fork,
+                                           cudaEventDisableTiming));
+        VFPS_CUDA(cudaEventCreateWithFlags(&b->join,
+                                           cudaEventDisableTiming));
         b->cur = 0;
         if (data) {
             size_t src = 0;
@@ -1605,6 +1638,15 @@ extern "C" int vfps_batch_destroy(vfps_batch* b)
     }
     cudaSetDevice(b->device);
     destroy_graphs(b);
+    if (b->fork) {
+        cudaEventDestroy(b->fork);
+    }
+    if (b->join) {
+        cudaEventDestroy(b->join);
+    }
+    if (b->side) {
+        cudaStreamDestroy(b->side);
+    }
     delete b;
     return VFPS_OK;
 }
