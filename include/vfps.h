@@ -409,9 +409,12 @@ VFPS_API int vfps_batch_get_csr(vfps_batch* batch, float* power,
  * F = -(rf + wake) the y-kick of row x, Phi its integral, d the drift
  * offset of column y, G its integral, T = slip0 / (dq dp).  The wake
  * depends on the profile: `iterations` fixed-point passes, each mixing
- * `mix` (0 < mix <= 1) of the new profile into the old.  change[nb]
- * (optional) receives the last relative L1 change of each profile
- * (0 for bunches without a wake; chain-1 bunches are left as they are). */
+ * `mix` (0 < mix <= 1) of the new profile into the old.  Members of a
+ * multi-bunch beam (vfps_batch_set_beams) iterate together: each pass
+ * sums, in every member's wake, the fields of all members' profiles of
+ * the previous pass at their bucket distances.  change[nb] (optional)
+ * receives the last relative L1 change of each profile (0 for bunches
+ * without a wake; chain-1 bunches are left as they are). */
 VFPS_API int vfps_batch_potential_well(vfps_batch* batch, uint32_t iterations,
                                        float mix, float* change);
 /* kernel launches per solver step (for launch accounting) */

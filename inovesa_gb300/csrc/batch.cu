@@ -1357,11 +1357,32 @@ extern "C" int vfps_batch_potential_well(vfps_batch* b, uint32_t iterations,
             static_cast<int>(smem)));
         DevBuf<float> ch(b->nb);
         VFPS_CUDA(cudaMemsetAsync(ch.p, 0, ch.bytes(), st));
-        k_potential_well<<<b->nb, THREADS, smem, st>>>(
-            b->bd.p, b->pw.p, b->pwtab.p, b->tabs.p, b->wt.p,
-            b->dens[b->cur].p, ch.p, b->ctx->d_status,
-            static_cast<int>(iterations), mix);
-        VFPS_LAUNCHED();
+        if (!b->coupled) {
+            // bunches on their own: every iteration in one launch
+            k_potential_well<<<b->nb, THREADS, smem, st>>>(
+                b->bd.p, b->pw.p, b->pwtab.p, b->tabs.p, b->wt.p,
+                b->beams.p, b->members.p, nullptr, nullptr,
+                b->dens[b->cur].p, ch.p, b->ctx->d_status,
+                static_cast<int>(iterations), mix, -1);
+            VFPS_LAUNCHED();
+        } else {
+            // coupled beams: one launch per iteration, the members'
+            // profiles of the previous pass in one buffer, the new ones
+            // in the other
+            DevBuf<float> pa(b->rows), pb(b->rows);
+            VFPS_CUDA(cudaMemsetAsync(pa.p, 0, pa.bytes(), st));
+            VFPS_CUDA(cudaMemsetAsync(pb.p, 0, pb.bytes(), st));
+            for (uint32_t it = 0; it <= iterations; it++) {
+                k_potential_well<<<b->nb, THREADS, smem, st>>>(
+                    b->bd.p, b->pw.p, b->pwtab.p, b->tabs.p, b->wt.p,
+                    b->beams.p, b->members.p, (it & 1) ? pb.p : pa.p,
+                    (it & 1) ? pa.p : pb.p, b->dens[b->cur].p, ch.p,
+                    b->ctx->d_status, static_cast<int>(iterations), mix,
+                    static_cast<int>(it));
+                VFPS_LAUNCHED();
+            }
+            VFPS_CUDA(cudaStreamSynchronize(st));   // before pa, pb go
+        }
         // profiles and filling of the new state (as after an upload)
         project_all(b, b->cur);
         integrate_all(b, b->cur, 0);

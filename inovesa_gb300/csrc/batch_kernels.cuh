@@ -251,6 +251,45 @@ __device__ __forceinline__ void load_toeplitz(const float* __restrict__ w,
     }
 }
 
+// The unscaled wake on rows x0 <= x < x0 + R of a bunch in beam Mb: the
+// fields of every member of the beam (the bunch included) at their bucket
+// distances, from the members' profiles in pin, into acc[x - x0] (each
+// thread sums the rows it owns).  W, partial, Pm: scratch as for
+// toeplitz_partials (Pm holds one member's profile of n cells).
+__device__ __forceinline__ void beam_wake_rows(
+    const BDev* __restrict__ bd, const BeamDev* __restrict__ beams,
+    const uint32_t* __restrict__ members, const BeamDev& Mb,
+    const float* __restrict__ w, int nmax, int n, int x0, int R,
+    const float* __restrict__ pin, float* W, float* partial, float* Pm,
+    float* acc)
+{
+    const int Q = THREADS / (R >> 3);
+    for (int x = threadIdx.x; x < R; x += THREADS) {
+        acc[x] = 0.f;
+    }
+    for (uint32_t k = 0; k < Mb.count; k++) {
+        const uint32_t b2 = members[Mb.first + k];
+        const BDev B2 = bd[b2];
+        const long long delta = (long long)(Mb.bucket - beams[b2].bucket)
+                                * Mb.spacing;
+        __syncthreads();   // the previous member's W, Pm, partial read
+        for (int i = threadIdx.x; i < n; i += THREADS) {
+            Pm[i] = pin[B2.prof_off + i];
+        }
+        load_toeplitz(w, nmax, n, W, delta + x0, R);
+        __syncthreads();
+        toeplitz_partials(Pm, W, partial, n, R);
+        __syncthreads();
+        for (int x = threadIdx.x; x < R; x += THREADS) {
+            float sum = 0.f;
+            for (int q = 0; q < Q; q++) {
+                sum += partial[size_t(q) * R + x];
+            }
+            acc[x] += sum;   // read back by this thread only
+        }
+    }
+}
+
 // One CTA per block of rows of a bunch (wake_block_rows; wblk: bunch and
 // first row of each CTA): wake potential of the previous step's profile on
 // the block's rows, charge integral, renormalisation factor and, for chain 0,
@@ -337,32 +376,8 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     if (sum_here && !coupled) {
         toeplitz_partials(P, W, partial, n, R);
     } else if (sum_here) {
-        // the fields of every member of the beam (this bunch included) at
-        // their bucket distances
-        for (int x = threadIdx.x; x < R; x += THREADS) {
-            acc[x] = 0.f;
-        }
-        for (uint32_t k = 0; k < Mb.count; k++) {
-            const uint32_t b2 = members[Mb.first + k];
-            const BDev B2 = bd[b2];
-            const long long delta = (long long)(Mb.bucket - beams[b2].bucket)
-                                    * Mb.spacing;
-            __syncthreads();   // the previous member's W, Pm, partial read
-            for (int i = threadIdx.x; i < n; i += THREADS) {
-                Pm[i] = pin[B2.prof_off + i];
-            }
-            load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, delta + xr0, R);
-            __syncthreads();
-            toeplitz_partials(Pm, W, partial, n, R);
-            __syncthreads();
-            for (int x = threadIdx.x; x < R; x += THREADS) {
-                float sum = 0.f;
-                for (int q = 0; q < Q; q++) {
-                    sum += partial[size_t(q) * R + x];
-                }
-                acc[x] += sum;   // read back by this thread only
-            }
-        }
+        beam_wake_rows(bd, beams, members, Mb, wt + B.wt_off, int(B.nmax), n,
+                       xr0, R, pin, W, partial, Pm, acc);
     }
     __syncthreads();   // partial sums, per-warp integrals and ticket_s
     FF tot = FF{0.f, 0.f};
@@ -525,7 +540,7 @@ struct PwDev {
 // for a mesh of n rows (every region grows with n, so the layout of the
 // largest mesh of a batch covers the others)
 struct PwSmem {
-    size_t P, W, partial, F, Phi, G, D, RF, WS, M, S, total;
+    size_t P, W, partial, F, Phi, G, D, RF, WS, M, S, acc, Pm, total;
 };
 
 __host__ __device__ inline PwSmem pw_smem(size_t n)
@@ -542,7 +557,9 @@ __host__ __device__ inline PwSmem pw_smem(size_t n)
     L.WS = L.RF + n;                  // Simpson weights [n]
     L.M = L.WS + n;                   // row maxima [n]
     L.S = L.M + n;                    // row sums [n]
-    L.total = L.S + n;
+    L.acc = L.S + n;                  // a beam's wake [n]
+    L.Pm = L.acc + n;                 // and one member's profile [n]
+    L.total = L.Pm + n;
     return L;
 }
 
@@ -635,17 +652,30 @@ __device__ float block_sum_f(float v, float* scratch32)
 // new profile into the old one).  One CTA per bunch; bunches of chain 1
 // are left as they are.  Writes the density normalised to the bunch's
 // filling and the last relative L1 change of the profile.
+// pass < 0: every iteration in this launch (bunches on their own).
+// pass >= 0 (a batch with coupled beams): iteration `pass` only; the wake
+// of each member sums the fields of its beam's profiles of the previous
+// pass (pin), the bunch's mixed profile goes to pout, and the last pass
+// (iters, or 0 without a wake) writes the density.
 __global__ void __launch_bounds__(THREADS)
 k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
                  const float* __restrict__ pwtab,
                  const float* __restrict__ tabs,
-                 const float* __restrict__ wt, float* __restrict__ dens,
-                 float* __restrict__ change, int* __restrict__ status,
-                 int iters, float mix)
+                 const float* __restrict__ wt,
+                 const BeamDev* __restrict__ beams,
+                 const uint32_t* __restrict__ members,
+                 const float* __restrict__ pin, float* __restrict__ pout,
+                 float* __restrict__ dens, float* __restrict__ change,
+                 int* __restrict__ status, int iters, float mix, int pass)
 {
     const BDev B = bd[blockIdx.x];
     if (B.chain != 0) {
         return;
+    }
+    const bool has_wake = B.flags & F_WAKE;
+    const int last = has_wake ? iters : 0;   // without a wake: one pass
+    if (pass > last) {
+        return;   // this bunch's state is written already
     }
     extern __shared__ float4 pwsm4[];
     __shared__ float scratch[32];
@@ -671,16 +701,17 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
     float* WS = base + L.WS;
     float* M = base + L.M;
     float* S = base + L.S;
+    float* acc = base + L.acc;
+    float* Pm = base + L.Pm;
     const PwDev Z = pw[blockIdx.x];
     const float* ws = tabs + B.tab_off + TAB_WS * n;
     for (int i = threadIdx.x; i < n; i += THREADS) {
         RF[i] = pwtab[Z.off + i];
         D[i] = pwtab[Z.off + n + i];
         WS[i] = ws[i];
-        P[i] = 0.f;
+        P[i] = pass > 0 ? pin[B.prof_off + i] : 0.f;
     }
-    const bool has_wake = B.flags & F_WAKE;
-    if (has_wake) {
+    if (has_wake && pass < 0) {
         load_toeplitz(wt + B.wt_off, int(B.nmax), n, W, 0, n);
     }
     __syncthreads();
@@ -701,19 +732,30 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Q = THREADS / (n >> 3);
     float delta = 0.f;
-    const int last = has_wake ? iters : 0;   // without a wake: one pass
-    for (int it = 0; it <= last; it++) {
+    bool changed = false;   // delta holds a change of this launch
+    const int it0 = pass < 0 ? 0 : pass;
+    const int it1 = pass < 0 ? last : pass;
+    for (int it = it0; it <= it1; it++) {
         // row kicks of the current profile (the first pass: RF only)
-        if (has_wake && it > 0) {
+        const bool wk = has_wake && it > 0;
+        if (wk && pass < 0) {
             toeplitz_partials(P, W, partial, n, n);
+        } else if (wk) {
+            beam_wake_rows(bd, beams, members, beams[blockIdx.x],
+                           wt + B.wt_off, int(B.nmax), n, 0, n, pin, W,
+                           partial, Pm, acc);
         }
         __syncthreads();
         for (int x = threadIdx.x; x < n; x += THREADS) {
             float wake = 0.f;
-            if (has_wake && it > 0) {
+            if (wk) {
                 float sum = 0.f;
-                for (int k = 0; k < Q; k++) {
-                    sum += partial[size_t(k) * n + x];
+                if (pass < 0) {
+                    for (int k = 0; k < Q; k++) {
+                        sum += partial[size_t(k) * n + x];
+                    }
+                } else {
+                    sum = acc[x];
                 }
                 wake = __fmul_rn(B.wakescale, sum);
             }
@@ -773,13 +815,17 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
             dsum += fabsf(r - P[x]);
             psum += fabsf(P[x]);
             P[x] = it == 0 ? r : fmaf(mix, r - P[x], P[x]);
+            if (pass >= 0) {
+                pout[B.prof_off + x] = P[x];
+            }
         }
         dsum = block_sum_f(dsum, scratch);
         psum = block_sum_f(psum, scratch);
         delta = psum > 0.f ? dsum / psum : 1.f;
+        changed = true;
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && (changed || pass < 0)) {
         change[blockIdx.x] = delta;
     }
 }

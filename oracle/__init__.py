@@ -370,6 +370,10 @@ def wake_potential(proj, Z, wakescaling, buckets=None, spacing=0,
     nmax = Z.size
     bk = np.ascontiguousarray(
         np.zeros(nb) if buckets is None else buckets, np.uint32)
+    # the padded profile holds every bunch at bucket * spacing
+    # (src/PS/ElectricField.cpp:255-263)
+    if int(bk.max()) * int(spacing) + n > nmax:
+        raise ValueError("bunches do not fit in the padded profile")
     wake = np.zeros((nb, n), dtype)
     pad = np.zeros(nmax, dtype)
     _fn("oracle_wake_potential", dtype)(

@@ -82,3 +82,45 @@ def state(p, Z, wakescaling, iterations=200, mix=0.5, fill=1.0):
                   if it > 0 else 1.0)
         rho = new if it == 0 else rho + mix * (new - rho)
     raise AssertionError("unreachable")
+
+
+def beam_states(p, Z, wakescaling, buckets, spacing, fills, iterations=200,
+                mix=0.5):
+    """(densities [member][x][y], last relative L1 changes) of the
+    potential-well start of a multi-bunch beam: the members share the
+    derived parameters p and one padded profile (their buckets `spacing`
+    mesh cells apart, src/PS/ElectricField.cpp:255-263), so each member's
+    wake carries the fields of all members' profiles of the previous
+    iteration; member m is normalised to fills[m]."""
+    n = p["ps_bins"]
+    nb = len(fills)
+    rf, dr, dq, dp, T = offsets(p)
+    wsx, wsy = _simpson(n, dq), _simpson(n, dp)
+    G = _trapezoid(dr)
+    G -= G.min()
+    rho = np.zeros((nb, n))
+    change = np.zeros(nb)
+    last = iterations if Z is not None else 0
+    for it in range(last + 1):
+        wake = (oracle.wake_potential(rho, Z, wakescaling, buckets=buckets,
+                                      spacing=spacing)
+                if Z is not None and it > 0 else np.zeros((nb, n)))
+        out = []
+        for m in range(nb):
+            F = -(rf + wake[m])
+            Phi = _trapezoid(F)
+            e = -(Phi[:, None] + G[None, :]
+                  + 0.5 * F[:, None] * dr[None, :]) / T
+            psi = np.exp(e - e.max())
+            psi *= fills[m] / np.einsum("xy,x,y->", psi, wsx, wsy)
+            out.append(psi)
+        if it == last:
+            return out, change
+        new = np.stack([psi @ wsy for psi in out])
+        if it > 0:
+            change = (np.abs(new - rho).sum(axis=1)
+                      / np.abs(rho).sum(axis=1))
+        else:
+            change = np.ones(nb)
+        rho = new if it == 0 else rho + mix * (new - rho)
+    raise AssertionError("unreachable")

@@ -88,3 +88,36 @@ def test_nearly_stationary_under_the_solver(gpu_ctx):
         c = np.stack([b.profile(i) for i in range(len(cases))])
         change[name] = np.abs(c - a).sum(1) / np.abs(a).sum(1)
     assert np.all(change["pw"] * 5 < change["gauss"]), change
+
+
+def test_coupled_beam_matches_restatement(gpu_ctx):
+    """A three-bunch beam (buckets 0, 1, 3 spaced 64 cells, free-space CSR
+    whose wake reaches the next buckets, filling shares 0.5/0.3/0.2) next
+    to a bunch on its own: every member's start against the beam
+    restatement (oracle.potential_well_ref.beam_states, the members'
+    fields of the previous iteration in each wake), the lone bunch against
+    its own; relative L1 <= 1e-4 as above.  The members' states differ
+    from their states alone by more than 1e-3, so the check sees the
+    coupling."""
+    p = P.derive(GridSize=64, StepsPerTs=200, padding=16.0, VacuumGap=-1.0,
+                 S_csr=0.5)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"], impedance=0)
+             for _ in range(4)]
+    b = V.BunchBatch(gpu_ctx, descs, [z])
+    fills = [0.5, 0.3, 0.2]
+    b.set_beams([1, 1, 1, 0], [0, 1, 3, 0], 64, fills + [1.0])
+    change = b.potential_well(iterations=150, mix=0.5)
+    ws = float(np.float32(descs[0].wakescaling))
+    want, _ = PW.beam_states(p, z.data(), ws, [0, 1, 3], 64, fills,
+                             iterations=150, mix=0.5)
+    for m in range(3):
+        got = b.density(m)
+        assert rel_l1(got, want[m]) <= 1e-4, (m, rel_l1(got, want[m]))
+        alone, _ = PW.state(p, z.data(), ws, iterations=150, fill=fills[m])
+        assert rel_l1(want[m], alone) > 1e-3
+        assert change[m] <= 1e-5
+    lone, _ = PW.state(p, z.data(), ws, iterations=150)
+    assert rel_l1(b.density(3), lone) <= 1e-4
+    assert np.allclose(b.filling(), fills + [1.0], rtol=1e-5)
+    assert gpu_ctx.device_status() == 0

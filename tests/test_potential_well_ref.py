@@ -17,8 +17,8 @@ from oracle import potential_well_ref as PW
 from inovesa_gb300 import params as P
 
 
-def setup(S, gap=0.0318, n=64, spt=200):
-    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=gap,
+def setup(S, gap=0.0318, n=64, spt=200, padding=2.0):
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=padding, VacuumGap=gap,
                  S_csr=S)
     w = P.wake_impedance_args(p)
     Z = oracle.make_impedance(w["nfreqs"], w["fmax"], w["R_bend"], w["frev"],
@@ -81,3 +81,42 @@ def test_nearly_stationary_under_the_reference_step():
         change[name] = np.abs(b - a).sum() / np.abs(a).sum()
         sim.close()
     assert change["pw"] * 5 < change["gauss"], change
+
+
+def beam_setup(S=0.5):
+    """64-row meshes with free-space CSR, whose wake reaches the next
+    buckets; a padded profile of 1024 cells for buckets 0, 1, 3 spaced 64
+    cells, and the wake scaling of the reference's current."""
+    p, Z = setup(S, gap=-1.0, padding=16.0)
+    ws = P.fill_desc(oracle.BunchDesc(), p, 0, Ib=p["Ib"]).wakescaling
+    return p, Z, ws
+
+
+def test_beam_of_one_is_the_bunch_state():
+    """A beam of one member is the single bunch's start, bit for bit in
+    FP64 (the same wake of the same profile)."""
+    p, Z, ws = beam_setup()
+    one, ch = PW.beam_states(p, Z, ws, [0], 0, [1.0], iterations=40)
+    ref, ch_ref = PW.state(p, Z, ws, iterations=40)
+    assert np.array_equal(one[0], ref)
+    assert ch[0] == ch_ref
+
+
+def test_beam_members_feel_each_other():
+    """Three members of a beam in buckets 0, 1, 3: the members' states
+    differ from their states alone by far more than the iteration's
+    floor, every state carries its filling share, and the iteration
+    settles."""
+    p, Z, ws = beam_setup()
+    fills = [0.5, 0.3, 0.2]
+    wsx = PW._simpson(64, (p["axes"][1] - p["axes"][0]) / 63)
+    wsy = PW._simpson(64, (p["axes"][4] - p["axes"][3]) / 63)
+    states, ch = PW.beam_states(p, Z, ws, [0, 1, 3], 64, fills,
+                                iterations=150)
+    diffs = []
+    for m, f in enumerate(fills):
+        alone, _ = PW.state(p, Z, ws, iterations=150, fill=f)
+        assert abs(np.einsum("xy,x,y->", states[m], wsx, wsy) - f) < 1e-12
+        diffs.append(np.abs(states[m] - alone).sum() / np.abs(alone).sum())
+    assert min(diffs) > 1e-3 and max(diffs) > 1e-2, diffs
+    assert np.all(ch < 1e-10)
