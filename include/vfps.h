@@ -398,8 +398,8 @@ VFPS_API int vfps_batch_set_csr(vfps_batch* batch,
  * holds (UINT64_MAX: not written yet). */
 VFPS_API int vfps_batch_get_csr(vfps_batch* batch, float* power,
                                 uint64_t* steps);
-/* Replace the density of every chain-0 bunch with the stationary state of
- * its solver step below the instability threshold, and refresh profiles
+/* Replace the density of every bunch with the stationary state of its
+ * solver step below the instability threshold, and refresh profiles
  * and filling (as vfps_batch_upload does).  The reference names this
  * start only as an ignored option (HaissinskiIterations,
  * src/IO/ProgramOptions.cpp:270); here it is the Haissinski potential
@@ -412,9 +412,12 @@ VFPS_API int vfps_batch_get_csr(vfps_batch* batch, float* power,
  * `mix` (0 < mix <= 1) of the new profile into the old.  Members of a
  * multi-bunch beam (vfps_batch_set_beams) iterate together: each pass
  * sums, in every member's wake, the fields of all members' profiles of
- * the previous pass at their bucket distances.  change[nb] (optional)
- * receives the last relative L1 change of each profile (0 for bunches
- * without a wake; chain-1 bunches are left as they are). */
+ * the previous pass at their bucket distances.  For the rotation chain
+ * (chain 1), rf and d are the linear kick and drift of the rotation's
+ * angle and only the wake kick enters the cross term, with the opposite
+ * sign: E = Phi + G + wake(x) d(y) / 2.  change[nb] (optional) receives
+ * the last relative L1 change of each profile (0 for bunches without a
+ * wake). */
 VFPS_API int vfps_batch_potential_well(vfps_batch* batch, uint32_t iterations,
                                        float mix, float* change);
 /* kernel launches per solver step (for launch accounting) */

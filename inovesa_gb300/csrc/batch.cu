@@ -62,7 +62,7 @@ struct vfps_batch {
     DevBuf<float> tabs, fp5, wt, dwt;
     DevBuf<RowStencil> st;
     DevBuf<PwDev> pw;          // potential-well state: per bunch
-    DevBuf<float> pwtab;       // raw RF and drift offsets of chain 0
+    DevBuf<float> pwtab;       // raw RF and drift offsets (potential well)
     DevBuf<uint32_t> row_bunch;
     DevBuf<float> dens[2], prof[2];
     DevBuf<float> wake, factor;
@@ -813,6 +813,20 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                 B.halo_hi = std::max(0, hi);
             } else {
                 const float ang = static_cast<float>(d.angle);
+                // the potential-well state of the rotation chain: the
+                // linear kick and drift of the rotation's angle (both axes
+                // in units of the spreads)
+                pwd.off = static_cast<uint32_t>(pwtab.size());
+                pwd.T = ang / (ax.delta * ay.delta);
+                pwd.chain = 1;
+                pwtab.resize(pwtab.size() + 2 * size_t(n), 0.f);
+                for (uint32_t x = 0; x < n; x++) {
+                    pwtab[pwd.off + x] = std::tan(ang) * (ax.zerobin
+                                                          - float(x));
+                }
+                for (uint32_t y = 0; y < n; y++) {
+                    pwtab[pwd.off + n + y] = ang * ay.v[y] / ax.delta;
+                }
                 B.cs = std::cos(-ang);
                 B.sn = std::sin(-ang);
                 const int h = (d.it - 1) / 2;

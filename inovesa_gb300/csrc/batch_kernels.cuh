@@ -532,8 +532,9 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
 // column) in pwtab, and the energy scale T of the state below
 struct PwDev {
     uint32_t off;  // rf offsets [n], then drift offsets [n]
-    float T;       // slip0 / (dq dp)
-    float pad[2];
+    float T;       // slip0 / (dq dp); 0: no potential-well state
+    uint32_t chain;
+    float pad;
 };
 
 // float offsets of the regions of k_potential_well's dynamic shared memory
@@ -639,7 +640,8 @@ __device__ float block_sum_f(float v, float* scratch32)
 }
 
 // The stationary state of the chain-0 step (y-kicks of the wake and the
-// RF, drift, Fokker-Planck) below the instability threshold: a function of
+// RF, drift, Fokker-Planck) below the instability threshold, and of the
+// rotation chain (rotation, wake kick, Fokker-Planck): a function of
 // the step's invariant, exp(-E / T) with
 //   E(x, y) = Phi(x) + G(y) + F(x) d(y) / 2,
 // F = -(rf + wake) the y-kick of row x (cells per step), Phi its integral
@@ -649,9 +651,12 @@ __device__ float block_sum_f(float v, float* scratch32)
 // (the continuous-time invariant); the cross term is the first correction
 // of the split step (kick, then drift) to it.  The wake depends on the
 // profile, so the profile iterates to a fixed point (mixing `mix` of each
-// new profile into the old one).  One CTA per bunch; bunches of chain 1
-// are left as they are.  Writes the density normalised to the bunch's
-// filling and the last relative L1 change of the profile.
+// new profile into the old one).  For the rotation chain, rf and d are the
+// linear kick and drift of the rotation's angle (its quadratic potential
+// and kinetic term) and only the wake kick enters the cross term, with the
+// opposite sign (the rotation conserves the radial invariant exactly; the
+// wake kick follows it).  One CTA per bunch.  Writes the density normalised
+// to the bunch's filling and the last relative L1 change of the profile.
 // pass < 0: every iteration in this launch (bunches on their own).
 // pass >= 0 (a batch with coupled beams): iteration `pass` only; the wake
 // of each member sums the fields of its beam's profiles of the previous
@@ -669,11 +674,17 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
                  int* __restrict__ status, int iters, float mix, int pass)
 {
     const BDev B = bd[blockIdx.x];
-    if (B.chain != 0) {
+    const PwDev Z = pw[blockIdx.x];
+    if (!(Z.T > 0.f)) {
         return;
     }
     const bool has_wake = B.flags & F_WAKE;
     const int last = has_wake ? iters : 0;   // without a wake: one pass
+    // half the row factor of the split-step term: the whole y-kick after
+    // the kick-drift step (chain 0); for the rotation chain only the wake
+    // kick, -(F + rf), with the sign of a kick after the rotation
+    const float hsign = Z.chain == 0 ? 0.5f : -0.5f;
+    const bool hrf = Z.chain != 0;
     if (pass > last) {
         return;   // this bunch's state is written already
     }
@@ -703,7 +714,6 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
     float* S = base + L.S;
     float* acc = base + L.acc;
     float* Pm = base + L.Pm;
-    const PwDev Z = pw[blockIdx.x];
     const float* ws = tabs + B.tab_off + TAB_WS * n;
     for (int i = threadIdx.x; i < n; i += THREADS) {
         RF[i] = pwtab[Z.off + i];
@@ -765,7 +775,8 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
         block_trapezoid(F, Phi, n, scratch);
         // per row: maximum of the exponent and the Simpson sum over y
         for (int x = warp; x < n; x += THREADS >> 5) {
-            const float phi = Phi[x], hf = 0.5f * F[x];
+            const float phi = Phi[x];
+            const float hf = hsign * (hrf ? F[x] + RF[x] : F[x]);
             float m = -3.4e38f;
             for (int y = lane; y < n; y += 32) {
                 m = fmaxf(m, -(phi + G[y] + hf * D[y]) * invT);
@@ -800,7 +811,8 @@ k_potential_well(const BDev* __restrict__ bd, const PwDev* __restrict__ pw,
             // the state: exp(-E / T) scaled to the filling
             float* out = dens + B.dens_off;
             for (int x = warp; x < n; x += THREADS >> 5) {
-                const float phi = Phi[x], hf = 0.5f * F[x];
+                const float phi = Phi[x];
+                const float hf = hsign * (hrf ? F[x] + RF[x] : F[x]);
                 for (int y = lane; y < n; y += 32) {
                     out[size_t(x) * n + y] =
                         scale * expf(-(phi + G[y] + hf * D[y]) * invT - mx);

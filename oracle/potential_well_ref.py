@@ -22,6 +22,12 @@ Baker-Campbell-Hausdorff term of the two maps).  The Fokker-Planck term
 holds the energy spread at one unit, which fixes the scale T = slip0 /
 (dq dp).  The density is exp(-E / T), the profile enters the wake, and
 the profile iterates to a fixed point.
+
+The rotation chain (chain 1) rotates the mesh exactly, which conserves the
+radial invariant; its state takes the rotation's quadratic potential and
+kinetic term as a linear kick and drift of the same angle, and only the
+wake kick enters the split-step term (with the sign of a kick after the
+rotation, the better of the two signs under the restated rotation step).
 """
 import numpy as np
 
@@ -41,12 +47,21 @@ def _trapezoid(f):
     return out
 
 
-def offsets(p):
+def offsets(p, chain=0):
     """(rf offsets per row, drift offsets per column, dq, dp, T) of the
-    chain-0 step of derived parameters p (inovesa_gb300.params.derive)."""
+    step of derived parameters p (inovesa_gb300.params.derive).  Chain 0:
+    the RF kick and the drift of the kick-drift step.  Chain 1 (the
+    rotation by `angle` per step, src/SM/RotationMap.cpp): the linear kick
+    and drift of the same angle (the rotation's quadratic potential and
+    kinetic term, in mesh cells, both axes in units of the spreads)."""
     n, axes, o = p["ps_bins"], p["axes"], p["opts"]
-    _, dq, _ = oracle.ruler(n, axes[0], axes[1])
-    _, dp, _ = oracle.ruler(n, axes[3], axes[4])
+    _, dq, zq = oracle.ruler(n, axes[0], axes[1])
+    pv, dp, _ = oracle.ruler(n, axes[3], axes[4])
+    if chain == 1:
+        th = p["angle"]
+        rf = np.tan(th) * (zq - np.arange(n))
+        dr = th * pv / dq
+        return rf, dr, dq, dp, th / (dq * dp)
     rf = oracle.rf_offsets(n, axes, bool(o["LinearRF"]), angle=p["angle"],
                            revpart=p["revolutionpart"], vrf=p["V_eff"],
                            v0=p["V0"], bl2phase=p["bl2phase"],
@@ -56,11 +71,19 @@ def offsets(p):
     return rf, dr, dq, dp, T
 
 
-def state(p, Z, wakescaling, iterations=200, mix=0.5, fill=1.0):
+def _cross(F, wake, chain):
+    """Half the row factor of the split-step term E += f(x) d(y): the whole
+    y-kick after the kick-drift step (chain 0); for the rotation chain only
+    the wake kick, with the sign of a kick that follows the rotation (the
+    rotation itself conserves the radial invariant exactly)."""
+    return 0.5 * F if chain == 0 else 0.5 * wake
+
+
+def state(p, Z, wakescaling, iterations=200, mix=0.5, fill=1.0, chain=0):
     """(density [x][y], last relative L1 change of the profile) of the
     potential-well start; Z the wake impedance (None: no wake)."""
     n = p["ps_bins"]
-    rf, dr, dq, dp, T = offsets(p)
+    rf, dr, dq, dp, T = offsets(p, chain)
     wsx, wsy = _simpson(n, dq), _simpson(n, dp)
     G = _trapezoid(dr)
     G -= G.min()
@@ -72,7 +95,8 @@ def state(p, Z, wakescaling, iterations=200, mix=0.5, fill=1.0):
                 if Z is not None and it > 0 else np.zeros(n))
         F = -(rf + wake)
         Phi = _trapezoid(F)
-        e = -(Phi[:, None] + G[None, :] + 0.5 * F[:, None] * dr[None, :]) / T
+        e = -(Phi[:, None] + G[None, :]
+              + _cross(F, wake, chain)[:, None] * dr[None, :]) / T
         psi = np.exp(e - e.max())
         psi *= fill / np.einsum("xy,x,y->", psi, wsx, wsy)
         if it == last:

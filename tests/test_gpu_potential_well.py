@@ -3,7 +3,8 @@
 
 Tolerance: relative L1 of each density <= 1e-4 (FP32 kernel, FP32 exp,
 against FP64); fixed-point change <= 1e-5 (the FP32 floor of the mixing
-iteration).  Bunches of chain 1 are left bit for bit as they were.  Then
+iteration); bunches of the rotation chain against the restatement's
+rotation-chain state.  Then
 the device's own solver step: one synchrotron period from the
 potential-well state moves the profile at least five times less than
 from the Gaussian start."""
@@ -49,17 +50,12 @@ def batch(ctx, cases, spt=1000):
 
 def test_matches_restatement(gpu_ctx):
     b, ps = batch(gpu_ctx, CASES)
-    nb = len(CASES)
-    before = [b.density(i).copy() for i in range(nb)]
     change = b.potential_well(iterations=200, mix=0.5)
     fill = b.filling()
     for i, (n, S, g, chain, wake) in enumerate(CASES):
         got = b.density(i)
-        if chain == 1:
-            assert np.array_equal(got, before[i])
-            continue
         p, Z, ws = ps[i]
-        want, _ = PW.state(p, Z, ws, iterations=200, mix=0.5)
+        want, _ = PW.state(p, Z, ws, iterations=200, mix=0.5, chain=chain)
         assert rel_l1(got, want) <= 1e-4, (i, rel_l1(got, want))
         assert change[i] <= 1e-5 if wake else change[i] == 0.0
         assert abs(fill[i] - 1.0) < 1e-5

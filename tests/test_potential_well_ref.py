@@ -83,6 +83,28 @@ def test_nearly_stationary_under_the_reference_step():
     assert change["pw"] * 5 < change["gauss"], change
 
 
+def test_rotation_chain_nearly_stationary():
+    """The rotation chain (src/main.cpp rotation loop: rotation with
+    clamping, wake kick, Fokker-Planck): one synchrotron period of the
+    restated step changes its potential-well state several times less
+    than the Gaussian start (the state's own change, about 1e-4 per period,
+    is the rotation's interpolation diffusion on this mesh)."""
+    p, Z = setup(0.3, gap=0.0318, n=256, spt=1000)
+    ws = P.wakescaling_for(p, p["Ib"])
+    start, _ = PW.state(p, Z, ws, chain=1)
+    change = {}
+    for name, data in (("pw", start), ("gauss", None)):
+        d = P.fill_desc(oracle.BunchDesc(), p, 1, Ib=p["Ib"], it=4,
+                        clamp=True)
+        sim = oracle.Sim([d], Z=Z, data=data, dtype=np.float64)
+        a = sim.density(0).copy()
+        sim.step(p["opts"]["StepsPerTs"], 4)
+        b = sim.density(0)
+        change[name] = np.abs(b - a).sum() / np.abs(a).sum()
+        sim.close()
+    assert change["pw"] * 10 < change["gauss"], change
+
+
 def beam_setup(S=0.5):
     """64-row meshes with free-space CSR, whose wake reaches the next
     buckets; a padded profile of 1024 cells for buckets 0, 1, 3 spaced 64
