@@ -366,7 +366,8 @@ void build_tiles(vfps_batch* b, int tile_cells)
         o = 0;
         take(&L.ring, size_t(rb) * L.rs * 4);
         take(&L.s, size_t(rows) * sizeof(RowInfo));
-        take(&L.bar, 2 * sizeof(uint64_t));
+        take(&L.tab, size_t(10) * n * 4);
+        take(&L.bar, 3 * sizeof(uint64_t));
         L.total = static_cast<uint32_t>(o);
         return o;
     };
@@ -886,7 +887,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                     }
                 }
                 // bunches of a scan share these tables: one copy each, so
-                // that they stay in L1
+                // that a ring kernel's CTA stages a shared one only once
                 std::string key(reinterpret_cast<const char*>(tab.data()),
                                 tab.size() * sizeof(float));
                 auto it = dw_seen.find(key);

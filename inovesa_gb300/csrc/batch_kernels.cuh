@@ -1275,7 +1275,8 @@ constexpr int RTHREADS = 128;
 struct SmemR {
     uint32_t ring;  // RB slots of RS floats
     uint32_t s;     // RowInfo of the new rows of one tile
-    uint32_t bar;   // two mbarriers
+    uint32_t tab;   // drift and Fokker-Planck planes of a bunch [10][n]
+    uint32_t bar;   // three mbarriers (two for the rows, one for tab)
     uint32_t rb;    // ring slots: twice the rows a tile reads
     uint32_t rs;    // floats per slot
     uint32_t total;
@@ -1435,7 +1436,7 @@ __device__ __forceinline__ void drift2(const float* ring, const RingMap& m,
                                        const float* __restrict__ W, int n,
                                        float* d0, float* d1)
 {
-    const int4 sh = __ldg(reinterpret_cast<const int4*>(W + 4 * n + y));
+    const int4 sh = *(reinterpret_cast<const int4*>(W + 4 * n + y));
     if (sh.x == sh.y && sh.y == sh.z && sh.z == sh.w) {
         // packed FP32 (two lanes of 4 columns per instruction; each
         // component rounds like fmaf / a plain product)
@@ -1449,7 +1450,7 @@ __device__ __forceinline__ void drift2(const float* ring, const RingMap& m,
             const float2 vb = make_float2(v.z, v.w);
             float4 wj = wp;
             if (j < 4) {
-                wj = __ldg(reinterpret_cast<const float4*>(W + j * n + y));
+                wj = *(reinterpret_cast<const float4*>(W + j * n + y));
             }
             const float2 wa = make_float2(wj.x, wj.y);
             const float2 wb = make_float2(wj.z, wj.w);
@@ -1539,7 +1540,7 @@ __device__ __forceinline__ void fp_rows2(const float* d0, const float* d1,
         float f[5][4];
 #pragma unroll
         for (int o = 0; o < 5; o++) {
-            const float4 v = __ldg(reinterpret_cast<const float4*>(
+            const float4 v = *(reinterpret_cast<const float4*>(
                 F + o * n + y));
             f[o][0] = v.x; f[o][1] = v.y; f[o][2] = v.z; f[o][3] = v.w;
         }
@@ -1605,7 +1606,7 @@ __device__ __forceinline__ void drift1(const float* ring, const RingMap& m,
                                        const float* __restrict__ W, int n,
                                        float* d)
 {
-    const int4 sh = __ldg(reinterpret_cast<const int4*>(W + 4 * n + y));
+    const int4 sh = *(reinterpret_cast<const int4*>(W + 4 * n + y));
     if (sh.x == sh.y && sh.y == sh.z && sh.z == sh.w) {
         // packed FP32 (each component rounds like fmaf / a plain product)
         float2 a = make_float2(0.f, 0.f), c = a;
@@ -1613,7 +1614,7 @@ __device__ __forceinline__ void drift1(const float* ring, const RingMap& m,
         for (int j = 0; j < 4; j++) {
             const float4 v = *reinterpret_cast<const float4*>(
                 ring + size_t(m.slot(X + sh.x + j, rb)) * rs + APAD + y);
-            const float4 w = __ldg(reinterpret_cast<const float4*>(
+            const float4 w = *(reinterpret_cast<const float4*>(
                 W + j * n + y));
             const float2 va = make_float2(v.x, v.y);
             const float2 vb = make_float2(v.z, v.w);
@@ -1680,7 +1681,7 @@ __device__ __forceinline__ float fp_row(const float (&d)[G][4], int l, int n,
         float f[5][4];
 #pragma unroll
         for (int q = 0; q < 5; q++) {
-            const float4 v = __ldg(reinterpret_cast<const float4*>(
+            const float4 v = *(reinterpret_cast<const float4*>(
                 F + q * n + y));
             f[q][0] = v.x;
             f[q][1] = v.y;
@@ -1739,6 +1740,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     char* base = reinterpret_cast<char*>(smem4);
     float* ring = reinterpret_cast<float*>(base + L.ring);
     RowInfo* S = reinterpret_cast<RowInfo*>(base + L.s);
+    float* T = reinterpret_cast<float*>(base + L.tab);
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
     const int rb = int(L.rb), rs = int(L.rs);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1755,6 +1757,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
         mbar_fence_init();
     }
     fence_proxy_async();
@@ -1774,9 +1777,25 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     RingMap mc{0}, mn{0};
     int lo_c = 0, hi_c = 0, lo_n = 0, hi_n = 0;
     int front = 0;   // ring position after the last staged row
+    // the drift and Fokker-Planck planes in T: those of table tab_off
+    // (bunches of one lattice share a table), a copy in flight while
+    // tab_wait, completing phase tab_ph of bar[2]
+    uint32_t tab_off = 0xffffffffu, tab_ph = 0;
+    bool tab_wait = false;
+    auto load_tab = [&](const BDev& Bt) {
+        const uint32_t bytes = 10u * Bt.n * 4u;
+        if (threadIdx.x == 0) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(&bar[2], bytes);
+            tma_load_1d(T, dwt + Bt.dw_off, bytes, &bar[2]);
+        }
+        tab_off = Bt.dw_off;
+        tab_wait = true;
+    };
     if (t_begin < t_end) {
         const Tile t = tiles[t_begin];
         const BDev B = bd[t.bunch];
+        load_tab(B);   // constant tables: before the wait below
         lo_c = int(t.x0) - B.halo_lo;
         hi_c = int(t.x0 + t.rows) + B.halo_hi;
         mc = RingMap::at(lo_c, 0);
@@ -1879,10 +1898,25 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             }
         }
 
+        // this tile's drift and Fokker-Planck planes in T (a new table is
+        // copied in after the barrier above, which ends the last tile's
+        // reads of the old one)
+        if (B.dw_off != tab_off) {
+            load_tab(B);
+        }
+        if (tab_wait) {
+            if (!mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS)) {
+                bad = 1;
+                mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS);
+            }
+            tab_ph ^= 1u;
+            tab_wait = false;
+        }
+
         // drift x-kick, Fokker-Planck, output rows and projections, two
         // rows per lane segment
         if constexpr (G == 2) {
-            const float* W = dwt + B.dw_off;      // drift planes [5][n]
+            const float* W = T;                   // drift planes [5][n]
             const float* F = W + 5 * n;           // Fokker-Planck [5][n]
             const float h03 = tabs[B.tab_off + TAB_WS * n];
             const int hw = seg >> 1;
@@ -1911,7 +1945,7 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             }
         } else {
             // one row per warp and pass, G groups of 4 columns per lane
-            const float* W = dwt + B.dw_off;      // drift planes [5][n]
+            const float* W = T;                   // drift planes [5][n]
             const float* F = W + 5 * n;           // Fokker-Planck [5][n]
             const float h03 = tabs[B.tab_off + TAB_WS * n];
             const int gw = n / G;
