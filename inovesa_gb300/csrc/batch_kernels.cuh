@@ -28,7 +28,7 @@ namespace {
 constexpr int THREADS = 256;
 constexpr int ROWPAD = 16;     // extra floats per rotated row (chain 1)
 constexpr int TPAD = 4;        // zero floats on each side of a t3 row
-constexpr int APAD = 16;       // zero floats left of a staged row (chain 0)
+constexpr int APAD = 8;        // zero floats left of a staged row (chain 0)
 constexpr uint64_t WAIT_NS = 1000000000ull;  // bounded TMA waits (1 s)
 
 struct __align__(16) BDev {     // 96 bytes: vector loads of its fields
