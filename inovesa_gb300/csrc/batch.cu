@@ -327,7 +327,7 @@ void build_tiles(vfps_batch* b, int tile_cells)
         int tx = std::max(4, tile_cells / n);
         if (c == TL_RING || c == TL_RING4) {
             // the ring holds two tiles with their halos: at most 32 staged
-            // rows per tile keeps it at 64 slots
+            // rows per tile keeps it at 64 slots or fewer
             tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
         }
         tx = std::min(tx, n);

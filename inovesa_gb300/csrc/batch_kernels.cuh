@@ -1,12 +1,14 @@
 // Device side of the batched solver step (included by batch.cu only).
 //
-//  k_bwake   one CTA per bunch: the wake potential of every mesh row as
-//            the Toeplitz sum  wake[x] = s sum_m P[m] w[(x-m) mod nmax]  of
-//            the previous step's profile P (w built once per impedance in
-//            FP64), the charge integral (compensated FP32), this step's
-//            renormalisation factor and the step counter.
+//  k_bwake   one CTA per bunch (per 128-row block of wider meshes): the
+//            wake potential of every mesh row as the Toeplitz sum
+//            wake[x] = s sum_m P[m] w[(x-m) mod nmax]  of the previous
+//            step's profile P (w built once per impedance in FP64), the
+//            charge integral (compensated FP32), this step's
+//            renormalisation factor, both y-kick stencils of every row and
+//            the step counter.
 //  k_bmaps0  chain 0 (the reference's loop, src/main.cpp:1034-1044) for
-//            meshes up to 256 rows: a persistent kernel whose CTAs walk
+//            meshes up to 512 rows: a persistent kernel whose CTAs walk
 //            consecutive tiles of mesh rows through a ring of staged rows
 //            in shared memory (TMA bulk copies one tile ahead); rows are
 //            y-kicked in place once, the drift x-kick and Fokker-Planck
@@ -1267,9 +1269,11 @@ k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
 // seg = n/8 consecutive lanes of one warp; lane l owns the two groups of 4
 // columns that start at 4l and n/2 + 4l, so that the lanes of a row read
 // and write consecutive 16-byte words (no shared-memory bank conflicts).
-// Staged rows live in a ring of RB slots (a power of two) of RS floats:
-// APAD zeros, the row, zeros; a tile's rows get the slots after the rows
-// staged before it, and consecutive tiles of a bunch share their halo rows.
+// Staged rows live in a ring of RB slots (twice the rows a tile reads) of
+// RS floats: APAD zeros, the row, zeros; a tile's rows get the slots after
+// the rows staged before it, and consecutive tiles of a bunch share their
+// halo rows.  The drift and Fokker-Planck planes of the tile's bunch sit
+// next to the ring (one bulk copy per distinct table).
 constexpr int RTHREADS = 128;
 
 struct SmemR {
