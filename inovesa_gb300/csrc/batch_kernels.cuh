@@ -1846,10 +1846,13 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             for (int i = rl; i < m; i += rp) {
                 const int x = lo_c + i;
                 float* row = ring + size_t(mc.slot(x, rb)) * rs;
-                // zeros right of the row (the slot may have held a longer
-                // row of another bunch)
-                for (int j = l; j < (APAD + 16) / 4; j += seg) {
-                    reinterpret_cast<float4*>(row + APAD + n)[j] = z;
+                // zeros right of the row: the slot may have held a longer
+                // row of another bunch (rows as long as the slots leave
+                // the zeros of the ring's start there)
+                if (n + 2 * APAD + 16 < rs) {
+                    for (int j = l; j < (APAD + 16) / 4; j += seg) {
+                        reinterpret_cast<float4*>(row + APAD + n)[j] = z;
+                    }
                 }
                 const int gw = n / G;   // columns per lane group
                 if (unsigned(x) < unsigned(n)) {
