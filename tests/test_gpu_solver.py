@@ -203,6 +203,30 @@ def test_short_tail_tile_beyond_halo(gpu_ctx, monkeypatch, n, cells, nb):
         assert rel_l1(got, ref.density(0)) <= TOL, i
 
 
+def test_batch_large_shifts(gpu_ctx):
+    """Few steps per period (50 on 256-row meshes): kick and drift offsets
+    up to 16 cells, so the kick windows of the edge columns reach past the
+    8 zero floats left of a staged row (the bounds-checked path) and the
+    halos are 17 rows deep (4-row tiles, an 80-slot ring).  Against the
+    FP64 oracle."""
+    n, spt = 256, 50
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=0.0318,
+                 S_csr=0.3)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    specs = [(p, 0, p["Ib"], 4, False), (p, 0, 0.5 * p["Ib"], 3, False)]
+    b = make_batch(gpu_ctx, specs, {n: z})
+    steps = 25
+    b.step(steps)
+    assert gpu_ctx.device_status() == 0
+    dens = b.download()
+    for i, (p_, ch, ib, it, cl) in enumerate(specs):
+        ref = oracle_sim(p_, ch, ib, z.data(), it=it, clamp=cl)
+        ref.step(steps)
+        off, _ = b.layout(i)
+        got = dens[off:off + n * n].reshape(n, n)
+        assert rel_l1(got, ref.density(0)) <= TOL, (i, rel_l1(got, ref.density(0)))
+
+
 def test_batch_rejects_wider_meshes(gpu_ctx):
     """Batched meshes go up to 1024 rows (the ring kernel); a 2048-row mesh
     is refused with a clear error (the plain path takes it)."""
