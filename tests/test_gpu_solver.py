@@ -227,6 +227,19 @@ def test_batch_large_shifts(gpu_ctx):
         assert rel_l1(got, ref.density(0)) <= TOL, (i, rel_l1(got, ref.density(0)))
 
 
+def test_batch_refuses_halos_beyond_shared_memory(gpu_ctx):
+    """512-row meshes at 60 steps per period: drift offsets of 27 cells
+    make a tile with its halo too deep for the ring in shared memory; the
+    batch is refused with an error instead of being launched."""
+    n, spt = 512, 60
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=0.0318,
+                 S_csr=0.3)
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    with pytest.raises(V.VfpsError, match="shared memory"):
+        make_batch(gpu_ctx, [(p, 0, p["Ib"], 4, False)], {n: z})
+    assert gpu_ctx.device_status() == 0
+
+
 def test_batch_rejects_wider_meshes(gpu_ctx):
     """Batched meshes go up to 1024 rows (the ring kernel); a 2048-row mesh
     is refused with a clear error (the plain path takes it)."""
