@@ -765,10 +765,11 @@ class BunchBatch(_Handle):
         return steps[ok][order].astype(np.int64), power[ok][order]
 
     def potential_well(self, iterations=200, mix=0.5):
-        """Replace every chain-0 density by the stationary state of its
-        step below threshold (the Haissinski potential well written in the
-        invariant of the discrete kick-drift step); returns the last
-        relative change of each profile in the fixed-point iteration."""
+        """Replace every density by the stationary state of its step below
+        threshold (the Haissinski potential well written in the invariant
+        of the discrete step: kick-drift, or rotation and wake kick; the
+        members of a coupled beam together); returns the last relative
+        change of each profile in the fixed-point iteration."""
         out = np.zeros(len(self.descs), np.float32)
         self._check(lib().vfps_batch_potential_well(
             self._h, int(iterations), float(mix), _fptr(out)))
