@@ -214,7 +214,7 @@ __device__ __forceinline__ void toeplitz_partials(const float* P,
         w[j] = W[k + (k >> 3)];
         acc[j] = 0.f;
     }
-#pragma unroll 4
+#pragma unroll 8   // a whole turn of the 8-register window: no moves
     for (int m = m0; m < m0 + span; m++) {
         const float pm = P[m];
 #pragma unroll
