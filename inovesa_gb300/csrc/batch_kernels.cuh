@@ -246,10 +246,16 @@ __device__ __forceinline__ void load_toeplitz(const float* __restrict__ w,
                                               int nmax, int n, float* W,
                                               long long delta, int R)
 {
+    // one 64-bit remainder per thread, then each step of k adds THREADS
+    // mod nmax to the index, and one subtraction reduces it
+    long long b = (delta + threadIdx.x - (n - 1)) % nmax;
+    b += b < 0 ? nmax : 0;
+    int base = static_cast<int>(b);
+    const int step = THREADS % nmax;
     for (int k = threadIdx.x; k < R + n - 1; k += THREADS) {
-        long long d = (delta + k - (n - 1)) % nmax;
-        d += d < 0 ? nmax : 0;
-        W[k + (k >> 3)] = w[d];
+        W[k + (k >> 3)] = w[base];
+        base += step;
+        base -= base >= nmax ? nmax : 0;
     }
 }
 
