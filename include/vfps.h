@@ -71,10 +71,13 @@ VFPS_API void* vfps_stream(vfps_ctx* ctx);
  * synchronises; *code is cleared afterwards. */
 VFPS_API int vfps_device_status(vfps_ctx* ctx, int* code);
 /* No reference counterpart: exercises the failure path of the solver
- * kernels' bounded waits without faulting the GPU.  One kernel waits on a
- * barrier that nothing completes, gives up after limit_ns (at most 1 s)
- * and sets the device status to VFPS_ERR_TIMEOUT; the context stays
- * usable (read and clear the status with vfps_device_status). */
+ * kernels' bounded waits without faulting the GPU.  One CTA walks 16
+ * tiles the way the persistent solver kernels do, each tile waiting on a
+ * barrier that nothing completes: the first wait gives up after limit_ns
+ * (at most 1 s), one more bounded wait follows, the CTA stops walking and
+ * sets the device status to VFPS_ERR_TIMEOUT, so the call ends after about
+ * 2 * limit_ns; the context stays usable (read and clear the status with
+ * vfps_device_status). */
 VFPS_API int vfps_selftest_wait_timeout(vfps_ctx* ctx, uint64_t limit_ns);
 /* Pinned host buffers for asynchronous copies (no reference counterpart). */
 VFPS_API int vfps_host_alloc(vfps_ctx* ctx, size_t bytes, void** ptr);
@@ -499,10 +502,14 @@ VFPS_API int vfps_ws_adam(vfps_ctx* ctx, float* w, const float* g, float* m,
  * Its scratch is one fixed __device__ array per device: at most 262144
  * rows (nb * n) and 4096 meshes per call, larger calls are rejected with
  * VFPS_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
- * scratch address once and should come before any stream capture starts.
- * Nothing in the scratch needs to start at zero.  Calls on one device must
- * not overlap in time (from several host threads, or several contexts on
- * one device): they share the scratch and would race on it. */
+ * scratch address once and should come before any stream capture starts;
+ * the address is tied to the device's context, so the first call after a
+ * device reset (cudaDeviceReset by the host program or a library) looks it
+ * up again and is a set-up call as well.  The call restores the calling
+ * thread's current device before it returns.  Nothing in the scratch
+ * needs to start at zero.  Calls on one device must not overlap in time
+ * (from several host threads, or several contexts on one device): they
+ * share the scratch and would race on it. */
 VFPS_API int vfps_charge_noalloc(vfps_ctx* ctx, const float* density,
                                  uint32_t nb, uint32_t n, float delta,
                                  double* integrals);

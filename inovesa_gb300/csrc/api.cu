@@ -199,19 +199,39 @@ extern "C" int vfps_device_status(vfps_ctx* ctx, int* code)
 }
 
 namespace {
-// One thread waits for the first phase of an mbarrier that nothing arrives
-// at, bounded by limit_ns like every wait of the solver kernels: the wait
-// gives up, records VFPS_ERR_TIMEOUT and the kernel returns (no copy in
-// flight, no tensor memory held).
-__global__ void k_wait_selftest(int* status, unsigned long long limit_ns)
+// The wait pattern of the persistent solver kernels on barriers that
+// nothing arrives at: a CTA walks `tiles` tiles; at each, every thread
+// waits for the tile's barrier phase, bounded by limit_ns, then waits once
+// more (for a copy that might still land); the CTA then decides together
+// (__syncthreads_or) and stops walking at the first tile whose wait ran
+// out, records VFPS_ERR_TIMEOUT and returns (no copy in flight, no tensor
+// memory held).  So the kernel ends after about two wait limits, not two
+// per tile.
+__global__ void k_wait_selftest(int* status, unsigned long long limit_ns,
+                                int tiles)
 {
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bar[2];
     if (threadIdx.x == 0) {
-        vfps::dev::mbar_init(&bar, 1);
+        vfps::dev::mbar_init(&bar[0], 1);
+        vfps::dev::mbar_init(&bar[1], 1);
         vfps::dev::mbar_fence_init();
-        if (!vfps::dev::mbar_wait_bounded(&bar, 0, limit_ns)) {
-            atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
+    }
+    __syncthreads();
+    int bad = 0;
+    for (int k = 0; k < tiles; k++) {
+        if (!vfps::dev::mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1,
+                                          limit_ns)) {
+            bad = 1;
+            vfps::dev::mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1,
+                                         limit_ns);
         }
+        if (__syncthreads_or(bad)) {
+            bad = 1;
+            break;
+        }
+    }
+    if (bad && threadIdx.x == 0) {
+        atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
     }
 }
 }  // namespace
@@ -226,7 +246,8 @@ extern "C" int vfps_selftest_wait_timeout(vfps_ctx* ctx, uint64_t limit_ns)
         return VFPS_ERR_INVALID_ARGUMENT;
     }
     return guard(ctx, [&] {
-        k_wait_selftest<<<1, 32, 0, ctx->stream>>>(ctx->d_status, limit_ns);
+        k_wait_selftest<<<1, 128, 0, ctx->stream>>>(ctx->d_status, limit_ns,
+                                                     16);
         VFPS_LAUNCHED();
         VFPS_CUDA(cudaStreamSynchronize(ctx->stream));
     });

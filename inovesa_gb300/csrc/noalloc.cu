@@ -23,9 +23,17 @@
 // results go to one file-scope __device__ array of fixed size (below).
 // Its address on a device is looked up once, by the first call made with
 // that device current (cudaGetSymbolAddress); make that first call before
-// any stream capture starts.  Calls whose nb * n rows or nb meshes exceed
-// the scratch are rejected with VFPS_ERR_INVALID_ARGUMENT before anything
-// is launched.
+// any stream capture starts.  The address belongs to the device's CUDA
+// context: it is remembered together with that context's unique id, and a
+// call that finds another context current (the host program or a library
+// reset the device with cudaDeviceReset and a new context came up) looks
+// it up again, so that call is a set-up call too.  Calls whose nb * n rows
+// or nb meshes exceed the scratch are rejected with
+// VFPS_ERR_INVALID_ARGUMENT before anything is launched.
+//
+// The call makes the context's device current while it runs and gives the
+// calling thread back the device that was current before (other entry
+// points of the library leave the context's device current).
 //
 // Rules for callers.  Nothing in the scratch has to start at zero: each
 // call writes every word it reads before reading it.  There is one scratch
@@ -52,6 +60,27 @@ constexpr int NOALLOC_THREADS = 256;
 
 std::mutex g_noalloc_mu;
 double* g_noalloc_ptr[NOALLOC_MAX_DEVICES] = {};
+// unique id of the context each cached address was looked up in
+unsigned long long g_noalloc_ctx[NOALLOC_MAX_DEVICES] = {};
+
+// cuCtxGetId of the driver (CUDA 12.0+), reached through the runtime so
+// that the library does not link the driver library itself
+using CtxGetIdFn = int (*)(void*, unsigned long long*);
+CtxGetIdFn ctx_get_id()
+{
+    static CtxGetIdFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000,
+                                             cudaEnableDefault, &q)
+                != cudaSuccess
+            || q != cudaDriverEntryPointSuccess) {
+            f = nullptr;
+        }
+        return reinterpret_cast<CtxGetIdFn>(f);
+    }();
+    return fn;
+}
 
 // Simpson weight of index i, computed as the host table of the PhaseSpace
 // path: h03 = delta / 3 at both ends, h03 * 4 at odd and h03 * 2 at even
@@ -114,19 +143,46 @@ int fail(vfps_ctx* ctx, int code, const char* msg)
     return code;
 }
 
-// the scratch address on the current device (looked up on first use)
+// the scratch address on the current device: looked up on the first call
+// in the device's current context (again after a device reset brought up
+// a new context; every call when the context id is not available)
 double* scratch_on(int device)
 {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[device]) {
+    unsigned long long id = 0;
+    const CtxGetIdFn get_id = ctx_get_id();
+    const bool known = get_id && get_id(nullptr, &id) == 0 && id != 0;
+    if (!g_noalloc_ptr[device] || !known || g_noalloc_ctx[device] != id) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) {
+            g_noalloc_ptr[device] = nullptr;
             return nullptr;
         }
         g_noalloc_ptr[device] = static_cast<double*>(p);
+        g_noalloc_ctx[device] = known ? id : 0;
     }
     return g_noalloc_ptr[device];
 }
+
+// makes a device current for the scope of one call and gives the calling
+// thread its previous device back
+struct DeviceScope {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceScope(int device)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            prev = -1;
+        }
+        ok = cudaSetDevice(device) == cudaSuccess;
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0) {
+            cudaSetDevice(prev);
+        }
+    }
+};
 
 }  // namespace
 
@@ -150,7 +206,8 @@ extern "C" int vfps_charge_noalloc(vfps_ctx* ctx, const float* density,
         return fail(ctx, VFPS_ERR_INVALID_ARGUMENT,
                     "vfps_charge_noalloc: device index out of range");
     }
-    if (cudaSetDevice(ctx->device) != cudaSuccess) {
+    const DeviceScope scope(ctx->device);
+    if (!scope.ok) {
         return fail(ctx, VFPS_ERR_CUDA, "vfps_charge_noalloc: cudaSetDevice");
     }
     double* scratch = scratch_on(ctx->device);

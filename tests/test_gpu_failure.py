@@ -1,9 +1,12 @@
 """Failure detection without a GPU fault.
 
-* A bounded wait that runs out: a kernel waits on a barrier that nothing
-  completes (vfps_selftest_wait_timeout); the wait gives up after its
-  limit, the device status reads VFPS_ERR_TIMEOUT, and the context keeps
-  working (a batch steps cleanly afterwards).
+* A bounded wait that runs out: a kernel walks 16 tiles waiting on
+  barriers that nothing completes (vfps_selftest_wait_timeout, the wait
+  pattern of the persistent solver kernels); the first wait gives up after
+  its limit and the CTA stops walking, so the call ends after about two
+  limits rather than two per tile; the device status reads
+  VFPS_ERR_TIMEOUT, and the context keeps working (a batch steps cleanly
+  afterwards).
 * The charge watchdog of the batched step: a bunch whose density carries
   no charge sets VFPS_ERR_NUMERIC (the reference throws on an
   unnormalisable filling, src/PS/PhaseSpace.cpp:47-51); after a valid
@@ -35,6 +38,15 @@ def test_bounded_wait_reports_timeout(gpu_ctx):
                                                      2_000_000),
                gpu_ctx.handle)
     assert time.perf_counter() - t0 < 5.0
+    assert gpu_ctx.device_status() == _lib.VFPS_ERR_TIMEOUT
+    # 100 ms limits: 16 tiles of two waits each would take 3.2 s; the
+    # early exit ends the walk after the first tile's two waits
+    t0 = time.perf_counter()
+    _lib.check(_lib.lib().vfps_selftest_wait_timeout(gpu_ctx.handle,
+                                                     100_000_000),
+               gpu_ctx.handle)
+    el = time.perf_counter() - t0
+    assert 0.19 < el < 1.0, el
     assert gpu_ctx.device_status() == _lib.VFPS_ERR_TIMEOUT
     assert gpu_ctx.device_status() == 0          # reading cleared it
     b = small_batch(gpu_ctx)

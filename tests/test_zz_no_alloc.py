@@ -6,7 +6,11 @@ Collected last (file name) so that it also runs after every other GPU
 test in the same process; it passes alone in a fresh process too.
 Tolerance: both paths add in the same order, so the FP64 integrals agree
 to 1e-12 relative; the PhaseSpace path hands per-bunch values out as
-float, compared at 1e-6 relative.
+float, compared at 1e-6 relative.  The calls at the scratch's limits are
+compared with an FP64 NumPy Simpson sum of the same data at 1e-6 relative
+(the device sums groups of 8 cells in FP32).  The property that makes the
+entry point worth having, that it allocates nothing, is checked through
+the device's free memory: unchanged across calls after the first.
 """
 import ctypes as C
 
@@ -48,6 +52,44 @@ def test_charge_noalloc_matches_phase_space(gpu_ctx):
         for v in got:
             s += v
         assert abs(s - total) <= 1e-12 * abs(total), (call, s, total)
+    assert gpu_ctx.device_status() == 0
+
+
+def simpson_charges(data, delta):
+    """FP64 Simpson integrals of meshes [nb][n][n] with the PhaseSpace
+    path's float weights (delta/3 at both ends, times 4 at odd and 2 at
+    even interior indices)."""
+    n = data.shape[-1]
+    h03 = np.float32(delta) / np.float32(3)
+    ws = np.where(np.arange(n) % 2 == 1, h03 * np.float32(4),
+                  h03 * np.float32(2)).astype(np.float32)
+    ws[0] = ws[-1] = h03
+    w = ws.astype(np.float64)
+    proj = data.astype(np.float64) @ w
+    return proj @ w
+
+
+@pytest.mark.parametrize("nb,n", [(1024, 256), (4096, 64)])
+def test_charge_noalloc_at_the_limits(gpu_ctx, nb, n):
+    """The largest accepted calls: every row of the scratch, and (4096
+    meshes) every per-mesh result slot; the device's free memory does not
+    change across the calls."""
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(nb + n)
+    data = rng.random((nb, n, n), dtype=np.float32)
+    dev = torch.from_numpy(data).to("cuda:0")
+    torch.cuda.synchronize()
+    delta = 12.0 / (n - 1)
+    want = simpson_charges(data, delta)
+    rc, got = noalloc(gpu_ctx, dev.data_ptr(), nb, n, delta)
+    assert rc == 0, _lib.lib().vfps_last_error(gpu_ctx.handle)
+    free0, _ = torch.cuda.mem_get_info(0)
+    for call in range(2):
+        rc, got = noalloc(gpu_ctx, dev.data_ptr(), nb, n, delta)
+        assert rc == 0, (call, _lib.lib().vfps_last_error(gpu_ctx.handle))
+        assert np.allclose(got, want, rtol=1e-6, atol=0), call
+        free1, _ = torch.cuda.mem_get_info(0)
+        assert free1 == free0, (call, free0, free1)
     assert gpu_ctx.device_status() == 0
 
 
