@@ -10,9 +10,13 @@ src/main.cpp:948-1053).  One bench step = one solver step of all bunches
 integrals; k_bmaps0: the fused maps and projections).  Synthetic data: the
 reference's Gaussian start.
 
-Prints one JSON line (rank 0).  --impl reference times the CPU
-restatement of the reference solver loop (the oracle, float) on all host
-cores on the same workload.
+Prints one JSON line (rank 0).  Besides the headline it carries, under
+"configs", the other workloads of the benchmark plan measured in the same
+run: the plain single bunch on the rotation chain (256x256, 500 steps per
+period), the bursting 512x512 bunch with CSR power every step, the uneven
+96-bunch batch and the headline scan on the rotation chain.  --impl
+reference times the CPU restatement of the reference solver loop (the
+oracle, float) on all host cores on the same workload.
 """
 import argparse
 import ctypes as C
@@ -45,6 +49,27 @@ def workload_params():
     p = P.derive(GridSize=GRID, StepsPerTs=SPT, padding=2.0, VacuumGap=gap)
     currents = np.geomspace(S_MIN, S_MAX, NB) * p["I_norm"]
     return p, gap, currents
+
+
+def uneven_workload(seed=4, nb=96, spt=2000):
+    """The uneven batch: nb bunches with mesh sides drawn from
+    {128, 256, 512, 1024}, currents S ~ U(0.1, 1.5) and interpolation
+    orders from {linear, quadratic, cubic} (2..4 points), seeded; the
+    parallel-plates gap is 0.006 of the bending radius.  Returns
+    [(derived parameters, order)] and the sorted mesh sizes."""
+    from inovesa_gb300 import params as P
+    rng = np.random.default_rng(seed)
+    sizes = rng.choice([128, 256, 512, 1024], size=nb)
+    cur = rng.uniform(0.1, 1.5, size=nb)
+    its = rng.choice([2, 3, 4], size=nb)
+    out = []
+    for n, S, it in zip(sizes, cur, its):
+        n, it = int(n), int(it)
+        p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+        p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                     VacuumGap=0.006 * p0["R_bend"], S_csr=float(S))
+        out.append((p, it))
+    return out, sorted(set(int(v) for v in sizes))
 
 
 def config_dict(p, gap, l2_note):
@@ -189,23 +214,39 @@ def cpu_baseline(p, currents, z, seconds=12.0):
             "single_core_value": GRID * GRID * s1 / el1}
 
 
-def accuracy_check(got, p, currents, z, total_steps):
-    """Density L1 of the batched FP32 result against the FP64 oracle for
-    the lowest-current bunch over the whole run (bunches in the bursting
-    regime are checked over short horizons by the tests: there FP32 and
-    FP64 trajectories separate exponentially)."""
+def accuracy_check(batch, start, p, currents, z, threads):
+    """Density L1 of the batched FP32 step against the FP64 oracle, from
+    the same Gaussian start, for a spread of the scan's bunches: S = 0.01,
+    0.1, 0.3, 0.6, 0.9, 1.2, 1.5 (the upper ones above the bursting
+    threshold, where FP32 and FP64 trajectories part exponentially, so the
+    comparison is made after every one of the first 10 steps and then at
+    25, 50 and 100 steps).  The whole 256-bunch batch steps (the
+    benchmark's own tiling); returns the worst L1 over the bunches and
+    checks, and the per-bunch L1 at 100 steps."""
     import oracle
     from inovesa_gb300 import params as P
-    out = {}
-    i0 = 0
-    d = P.fill_desc(oracle.BunchDesc(), p, 0, Ib=float(currents[i0]))
-    ref = oracle.Sim([d], Z=z, dtype=np.float64)
-    ref.step(total_steps, threads=1)
-    want = ref.density(0)
-    out["low_current_l1"] = float(np.abs(got - want).sum()
-                                  / np.abs(want).sum())
-    out["low_current_steps"] = int(total_steps)
-    return out
+    s_norm = np.asarray(currents) / p["I_norm"]
+    targets = (0.01, 0.1, 0.3, 0.6, 0.9, 1.2, 1.5)
+    idx = [int(np.argmin(np.abs(s_norm - s))) for s in targets]
+    descs = [P.fill_desc(oracle.BunchDesc(), p, 0, Ib=float(currents[i]))
+             for i in idx]
+    ref = oracle.Sim(descs, Z=z, dtype=np.float64)
+    batch.upload(start)
+    worst, done, last = 0.0, 0, {}
+    for check in list(range(1, 11)) + [25, 50, 100]:
+        batch.step(check - done)
+        ref.step(check - done, threads=threads)
+        done = check
+        for k, i in enumerate(idx):
+            want = ref.density(k)
+            got = batch.density(i).astype(np.float64)
+            err = float(np.abs(got - want).sum() / np.abs(want).sum())
+            worst = max(worst, err)
+            last[k] = err
+    return {"max_l1": worst, "bar": 1e-4,
+            "steps_checked": "1..10, 25, 50, 100 from the Gaussian start",
+            "bunches": [{"S": float(s_norm[i]), "l1_at_100": last[k]}
+                        for k, i in enumerate(idx)]}
 
 
 def run_reference(args):
@@ -249,179 +290,210 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def other_workload(args):
-    """The other workloads of the benchmark plan, one JSON line each (not
-    the headline): plain single bunch (256x256, cubic rotation chain, 500
-    steps per period, free-space CSR, S = 0.05), bursting (512x512,
-    parallel-plates CSR + resistive wall, 4000 steps per period, S = 1.2,
-    CSR power every step), uneven batch (96 seeded bunches of 128..1024,
-    orders 2..4, S ~ U(0.1, 1.5), 2000 steps per period)."""
+def rel_l1(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.abs(a - b).sum() / np.abs(b).sum())
+
+
+def plain_driver(p, chain, it, clamp, steps, warmup, csr=False, Ib=None):
+    """The plain one-map-per-launch GPU loop timed inside the C++ driver
+    (inovesa_gb300/cpp/vfps_solver.cpp: the reference's main.cpp loop over
+    include/vfps.hpp, no interpreter in the loop).  Returns cell-updates/s
+    of the timed steps and the density after warmup + steps."""
+    from inovesa_gb300 import build as B
+    from inovesa_gb300 import params as P
+    exe = B.build_driver()
+    n = p["ps_bins"]
+    with tempfile.TemporaryDirectory() as d:
+        rf = os.path.join(d, "run.txt")
+        with open(rf, "w") as f:
+            f.write(P.run_file(p, chain=chain, it=it, clamp=clamp,
+                               steps=steps, csr=csr, warmup=warmup, Ib=Ib))
+        out = os.path.join(d, "out")
+        r = subprocess.run([exe, rf, out], capture_output=True, text=True,
+                           timeout=900)
+        if r.returncode != 0:
+            raise RuntimeError("vfps_solver failed: " + r.stderr)
+        with open(out + ".timing") as f:
+            st, sec = f.read().split()
+        dens = np.fromfile(out + ".density", np.float32).reshape(n, n)
+    return n * n * int(st) / float(sec), dens
+
+
+def cpu_rate(descs, Z, seconds, threads):
+    """The oracle's float restatement of the reference loop on the host
+    cores: cell-updates/s over about `seconds`, and the steps sampled."""
+    import oracle
+    sim = oracle.Sim(descs, Z=Z, dtype=np.float32)
+    t = time.perf_counter()
+    sim.step(2, threads=threads)
+    per = max((time.perf_counter() - t) / 2, 1e-4)
+    k = max(2, int(seconds / per))
+    t = time.perf_counter()
+    sim.step(k, threads=threads)
+    cells = sum(int(d.n) ** 2 for d in descs) * k
+    return cells / (time.perf_counter() - t), k
+
+
+def timed_batch(b, stream, steps, warmup):
+    """cell-updates/s of back-to-back batched steps (CUDA events on the
+    library's stream)."""
     import torch
-    import __graft_entry__
-    __graft_entry__.build()
+    b.step(warmup)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.step(steps)
+    e1.record(stream)
+    e1.synchronize()
+    return b.cells * steps / (e0.elapsed_time(e1) / 1e3)
+
+
+def config_plain_rotation(ctx, hbm):
+    """Plain single bunch: 256x256, cubic RotationMap with clamping, 500
+    steps per period, damping time 100 periods, free-space CSR, S = 0.05,
+    two synchrotron periods: the plain GPU loop (C++ driver), its density
+    against FP64 after the two periods, one host core."""
     import oracle
     from inovesa_gb300 import params as P
     from inovesa_gb300 import vfps as V
-    from inovesa_gb300.solver import PlainSolver
-    ctx = V.Context(0)
-    stream = torch.cuda.ExternalStream(
-        __import__("inovesa_gb300._lib", fromlist=["lib"]).lib().vfps_stream(
-            ctx.handle), device=0)
-    cores = os.cpu_count() or 1
-    out = {"workload": args.workload, "unit": "cell-updates/s",
-           "metric": METRIC}
+    n, spt = 256, 500
+    fs = P.derive(GridSize=n, StepsPerTs=spt)["fs"]
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=-1.0,
+                 S_csr=0.05, DampingTime=100.0 / fs)
+    total, warm = 2 * spt, 20
+    rate, dens = plain_driver(p, 1, 4, True, total - warm, warm)
+    z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+    d = P.fill_desc(oracle.BunchDesc(), p, 1, Ib=p["Ib"], it=4, clamp=True)
+    ref = oracle.Sim([d], Z=z.data(), dtype=np.float64)
+    ref.step(total)
+    cpu1, k1 = cpu_rate([d], z.data(), 3.0, 1)
+    return {"workload": "plain single bunch 256x256, cubic RotationMap "
+                        "(clamped), 500 steps/period, damping 100 periods, "
+                        "free-space CSR, S=0.05, 2 periods",
+            "gpu_plain": rate,
+            "gpu_plain_driver": "C++ (include/vfps.hpp), one map per launch",
+            "density_l1_vs_fp64": rel_l1(dens, ref.density(0)),
+            "accuracy_steps": total, "cpu_1core": cpu1,
+            "cpu_sample": "%d solver steps, 1 thread" % k1}
 
-    def time_plain(s, n, steps, csr=False):
-        s.step(10, csr=csr)
-        ctx.synchronize()
-        t = time.perf_counter()
-        s.step(steps, csr=csr)
-        ctx.synchronize()
-        return n * n * steps / (time.perf_counter() - t)
 
-    def time_oracle(descs, Z, seconds, threads):
-        sim = oracle.Sim(descs, Z=Z, dtype=np.float32)
-        t = time.perf_counter()
-        sim.step(2, threads=threads)
-        per = max((time.perf_counter() - t) / 2, 1e-4)
-        k = max(2, int(seconds / per))
-        t = time.perf_counter()
-        sim.step(k, threads=threads)
-        cells = sum(int(d.n) ** 2 for d in descs) * k
-        return cells / (time.perf_counter() - t), k
+def config_bursting(ctx, stream, hbm):
+    """Bursting: 512x512, parallel-plates CSR (g/R = 0.006) + resistive
+    wall (5.8e7 S/m), 4000 steps per period, S = 1.2, CSR power every step:
+    the plain GPU loop (C++ driver), the batched step on that bunch and on
+    a 32-bunch bursting scan (S 0.8..1.6), all with the CSR power of every
+    bunch every step; densities against FP64 after 200 steps."""
+    import oracle
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    n, spt, S = 512, 4000, 1.2
+    p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                 VacuumGap=0.006 * p0["R_bend"], S_csr=S,
+                 WallConductivity=5.8e7)
+    total, warm = 200, 20
+    rate, dens = plain_driver(p, 0, 4, False, total - warm, warm, csr=True)
+    z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+    zr = V.makeImpedance(ctx, **P.csr_impedance_args(p))
+    d = P.fill_desc(oracle.BunchDesc(), p, 0, Ib=p["Ib"], it=4)
+    ref = oracle.Sim([d], Z=z.data(), dtype=np.float64)
+    ref.step(total)
+    out = {"workload": "bursting 512x512, parallel-plates CSR g/R=0.006 + "
+                       "resistive wall, 4000 steps/period, S=1.2, CSR power "
+                       "every step",
+           "gpu_plain": rate,
+           "gpu_plain_driver": "C++ (include/vfps.hpp), one map per launch",
+           "plain_density_l1_vs_fp64": rel_l1(dens, ref.density(0)),
+           "accuracy_steps": total}
 
-    if args.workload in ("plain", "bursting"):
-        if args.workload == "plain":
-            n, spt, chain, S = 256, 500, 1, 0.05
-            fs = P.derive(GridSize=n, StepsPerTs=spt)["fs"]
-            p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
-                         VacuumGap=-1.0, S_csr=S, DampingTime=100.0 / fs)
-            csr, clamp = False, True
-        else:
-            n, spt, chain, S = 512, 4000, 0, 1.2
-            p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
-            p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
-                         VacuumGap=0.006 * p0["R_bend"], S_csr=S,
-                         WallConductivity=5.8e7)
-            csr, clamp = True, False
-        z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
-        zr = (V.makeImpedance(ctx, **P.csr_impedance_args(p)) if csr
-              else None)
-        s = PlainSolver(ctx, p, chain=chain, wake_impedance=z,
-                        csr_impedance=zr, it=4, clamp=clamp)
-        out["gpu_plain"] = time_plain(s, n, args.steps, csr)
-        d = P.fill_desc(oracle.BunchDesc(), p, chain, Ib=p["Ib"], it=4,
-                        clamp=clamp)
-        v1, k1 = time_oracle([d], z.data(), 10.0, 1)
-        out["cpu_1core"] = v1
-        out["cpu_sample"] = "%d solver steps of the bunch, 1 thread" % k1
-        # accuracy of the plain GPU loop against FP64 over 2 periods
-        s2 = PlainSolver(ctx, p, chain=chain, wake_impedance=z, it=4,
-                         clamp=clamp)
-        ref = oracle.Sim([d], Z=z.data(), dtype=np.float64)
-        steps = 2 * spt if args.workload == "plain" else 200
-        s2.step(steps)
-        ref.step(steps)
-        want = ref.density(0)
-        out["density_l1_vs_fp64"] = float(
-            np.abs(s2.density() - want).sum() / np.abs(want).sum())
-        out["accuracy_steps"] = steps
-        out["config"] = {"grid": n, "steps_per_period": spt, "S": S,
-                         "chain": chain, "csr_every_step": csr}
-        if args.workload == "bursting":
-            # the batched step on the same bunch, and on a bursting scan of
-            # 32 such bunches (S log-spaced 0.8..1.6), with every bunch's
-            # CSR power recorded every step
-            def batched(currents):
-                descs = [P.fill_desc(V.BunchDesc(), p, 0,
-                                     Ib=p["Ib"] * c / S, impedance=0)
-                         for c in currents]
-                b = V.BunchBatch(ctx, descs, [z])
-                nbb = len(currents)
-                b.set_csr([zr], [0] * nbb, [p["fc"]] * nbb,
-                          [P.C / p["bl"]] * nbb, every=1, capacity=8)
-                b.step(args.warmup)
-                ctx.synchronize()
-                e0 = torch.cuda.Event(enable_timing=True)
-                e1 = torch.cuda.Event(enable_timing=True)
-                e0.record(stream)
-                b.step(args.steps)
-                e1.record(stream)
-                e1.synchronize()
-                return b, b.cells * args.steps / (e0.elapsed_time(e1) / 1e3)
-            b1, out["gpu_batched_one"] = batched([S])
-            _, out["gpu_batched_scan32"] = batched(
-                list(np.geomspace(0.8, 1.6, 32)))
-            b3, _ = batched([S])
-            before = b3.download().reshape(n, n).copy()
-            ref3 = oracle.Sim([d], Z=z.data(), data=before,
-                              dtype=np.float64)
-            b3.step(200)
-            ref3.step(200)
-            # shapes at equal charge (the oracle normalises the state it
-            # is given; the batch's charge has drifted by ~1e-5 by then)
-            want = ref3.density(0)
-            got = b3.density(0).astype(np.float64)
-            got *= want.sum() / got.sum()
-            out["batched_density_l1_vs_fp64"] = float(
-                np.abs(got - want).sum() / np.abs(want).sum())
-            out["batched_note"] = ("batched rates include the CSR power of "
-                                   "every bunch every step")
-    else:
-        rng = np.random.default_rng(4)
-        nb, spt = 96, 2000
-        sizes = rng.choice([128, 256, 512, 1024], size=nb)
-        cur = rng.uniform(0.1, 1.5, size=nb)
-        its = rng.choice([2, 3, 4], size=nb)
-        keys = sorted(set(int(v) for v in sizes))
-        zs = {}
-        for k in keys:
-            p0 = P.derive(GridSize=k, StepsPerTs=spt, padding=2.0)
-            pk = P.derive(GridSize=k, StepsPerTs=spt, padding=2.0,
-                          VacuumGap=0.006 * p0["R_bend"])
-            zs[k] = V.makeImpedance(ctx, **P.wake_impedance_args(pk))
-        descs, ps = [], []
-        for n, S, it in zip(sizes, cur, its):
-            n, it = int(n), int(it)
-            p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
-            p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
-                         VacuumGap=0.006 * p0["R_bend"], S_csr=float(S))
-            ps.append((p, it))
-            descs.append(P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"],
-                                     impedance=keys.index(n), it=it))
-        b = V.BunchBatch(ctx, descs, [zs[k] for k in keys])
-        b.step(args.warmup)
-        ctx.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        b.step(args.steps)
-        e1.record(stream)
-        e1.synchronize()
-        ms = e0.elapsed_time(e1)
-        out["gpu_batched"] = b.cells * args.steps / (ms / 1e3)
-        out["kernel_ms_per_step"] = b.kernel_times(20)
-        out["cells_per_step"] = int(sum(int(v) ** 2 for v in sizes))
-        # the plain loop, one bunch at a time, on one bunch of each size
-        rates = []
-        for k in keys:
-            i = int(np.nonzero(sizes == k)[0][0])
-            p, it = ps[i]
-            s = PlainSolver(ctx, p, chain=0, wake_impedance=zs[k], it=it)
-            rates.append((k, time_plain(s, k, 200)))
-        # whole batch one bunch after another at those rates
-        t_plain = sum(int(n) ** 2 / dict(rates)[int(n)] for n in sizes)
-        out["gpu_plain"] = out["cells_per_step"] / t_plain
-        od = [P.fill_desc(oracle.BunchDesc(), p, 0, Ib=p["Ib"], it=it)
-              for p, it in ps[:max(cores, 1)]]
-        vv, kk = time_oracle(od, None, 12.0, cores)
-        out["cpu_all_cores"] = vv
-        out["cpu_cores"] = cores
-        out["cpu_sample"] = ("%d bunches of the batch, %d steps, no wake, "
-                             "%d threads" % (len(od), kk, cores))
-        out["config"] = {"bunches": nb, "sizes": "seeded 128..1024",
-                         "steps_per_period": spt}
-    print(json.dumps(out), flush=True)
+    def batch(currents):
+        descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"] * c / S,
+                             impedance=0) for c in currents]
+        b = V.BunchBatch(ctx, descs, [z])
+        m = len(currents)
+        b.set_csr([zr], [0] * m, [p["fc"]] * m, [P.C / p["bl"]] * m,
+                  every=1, capacity=8)
+        return b
+    b1 = batch([S])
+    out["gpu_batched_one"] = timed_batch(b1, stream, 200, 10)
+    bs = batch(list(np.geomspace(0.8, 1.6, 32)))
+    out["gpu_batched_scan32"] = timed_batch(bs, stream, 100, 5)
+    kt = bs.kernel_times(20)
+    out["scan32_kernel_ms_per_step"] = kt
+    out["scan32_maps_hbm_frac"] = 8.0 * bs.cells / (kt["k_bmaps0"] / 1e3) \
+        / 1e9 / hbm
+    b3 = batch([S])
+    b3.step(total)
+    out["batched_density_l1_vs_fp64"] = rel_l1(b3.density(0),
+                                               ref.density(0))
+    out["cpu_1core"], k1 = cpu_rate([d], z.data(), 3.0, 1)
+    out["cpu_sample"] = "%d solver steps, 1 thread" % k1
+    return out
+
+
+def config_uneven(ctx, stream, hbm, cores):
+    """Uneven batch: 96 seeded bunches of 128..1024 rows, S ~ U(0.1, 1.5),
+    orders 2..4, 2000 steps per period (38.5 M cells per step, larger than
+    L2): batched rate, per-kernel times, the chain-0 maps' HBM fraction,
+    the plain loop (C++ driver, one bunch of each size, weighted by the
+    batch's mix), a host-core sample."""
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    ps, keys = uneven_workload(4, 96, 2000)
+    sizes = np.array([p["ps_bins"] for p, _ in ps])
+    zs = {}
+    for k in keys:
+        pk = next(p for p, _ in ps if p["ps_bins"] == k)
+        zs[k] = V.makeImpedance(ctx, **P.wake_impedance_args(pk))
+    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"],
+                         impedance=keys.index(p["ps_bins"]), it=it)
+             for p, it in ps]
+    b = V.BunchBatch(ctx, descs, [zs[k] for k in keys])
+    out = {"workload": "uneven batch: 96 bunches, meshes 128..1024 "
+                       "(seeded), S~U(0.1,1.5), orders 2..4, 2000 "
+                       "steps/period",
+           "cells_per_step": int(b.cells),
+           "gpu_batched": timed_batch(b, stream, 50, 5)}
+    kt = b.kernel_times(20)
+    out["kernel_ms_per_step"] = kt
+    out["maps_hbm_frac"] = 8.0 * b.cells / (kt["k_bmaps0"] / 1e3) / 1e9 / hbm
+    rates = {}
+    for k in keys:
+        i = int(np.nonzero(sizes == k)[0][0])
+        p, it = ps[i]
+        rates[k], _ = plain_driver(p, 0, it, False, 100, 10)
+    t_plain = sum(int(n) ** 2 / rates[int(n)] for n in sizes)
+    out["gpu_plain"] = b.cells / t_plain
+    out["gpu_plain_driver"] = ("C++ (include/vfps.hpp), one bunch of each "
+                               "size, weighted by the batch")
+    import oracle
+    od = [P.fill_desc(oracle.BunchDesc(), p, 0, Ib=p["Ib"], it=it)
+          for p, it in ps[:max(cores, 1)]]
+    out["cpu_all_cores"], kk = cpu_rate(od, None, 4.0, cores)
+    out["cpu_sample"] = ("%d bunches of the batch, %d steps, no wake, %d "
+                         "threads" % (len(od), kk, cores))
+    return out
+
+
+def config_scan_rotation(ctx, stream, hbm, p, currents, z):
+    """The current scan of the headline on the rotation chain (cubic
+    RotationMap, wake kick, Fokker-Planck; the batched k_bmaps1): rate,
+    kernel times and the maps kernel's HBM fraction."""
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    descs = [P.fill_desc(V.BunchDesc(), p, 1, Ib=float(ib), impedance=0)
+             for ib in currents]
+    b = V.BunchBatch(ctx, descs, [z])
+    out = {"workload": "the headline's 256-bunch scan on the rotation "
+                       "chain (cubic RotationMap, wake kick, "
+                       "Fokker-Planck)",
+           "gpu_batched": timed_batch(b, stream, 50, 5)}
+    kt = b.kernel_times(20)
+    out["kernel_ms_per_step"] = kt
+    out["maps_hbm_frac"] = 8.0 * b.cells / (kt["k_bmaps1"] / 1e3) / 1e9 / hbm
+    return out
 
 
 def main():
@@ -432,10 +504,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=100)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="scan",
-                    choices=["scan", "plain", "bursting", "uneven"],
-                    help="scan: the headline line; the others print one "
-                         "line of their own")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the other workloads of the benchmark plan "
+                         "(the \"configs\" key)")
     ap.add_argument("--wake-mode", type=int, default=0, choices=[0, 1],
                     help="wake potentials on the CUDA cores (0) or the "
                          "tensor cores (1); the other mode is measured "
@@ -446,12 +517,10 @@ def main():
     args = ap.parse_args()
     if args.profile:
         args.no_cpu = True
+        args.no_configs = True
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
-        return
-    if args.workload != "scan":
-        other_workload(args)
         return
 
     rank = int(os.environ.get("RANK", "0"))
@@ -469,7 +538,6 @@ def main():
     from inovesa_gb300 import _lib
     from inovesa_gb300 import params as P
     from inovesa_gb300 import vfps as V
-    from inovesa_gb300.solver import PlainSolver
 
     p, gap, currents = workload_params()
     ctx = V.Context(local)
@@ -491,6 +559,7 @@ def main():
         with torch.cuda.stream(stream):
             flush.fill_(1.0)
 
+    start = batch.download()   # the Gaussian start (accuracy check)
     batch.step(args.warmup)
     ctx.synchronize()
     if dist:
@@ -520,7 +589,6 @@ def main():
         print(json.dumps({"error": "device status %d after the timed steps"
                           % status}), flush=True)
         sys.exit(3)
-    snap_low = batch.density(0)
     if args.profile:
         if rank == 0:
             print(json.dumps({"profile_run": True, "value": value,
@@ -597,21 +665,14 @@ def main():
     for h in (hin, hout, hprof, hfill):
         _lib.check(L.vfps_host_free(ctx.handle, h))
 
-    # plain one-map-per-launch loop, one bunch at a time
-    plain = PlainSolver(ctx, p, chain=0, wake_impedance=z,
-                        Ib=float(currents[NB // 2]))
-    plain.step(20)
-    ctx.synchronize()
-    t = time.perf_counter()
-    nplain = 300
-    plain.step(nplain)
-    ctx.synchronize()
-    plain_value = GRID * GRID * nplain / (time.perf_counter() - t)
-
     if rank != 0:
         if dist:
             dist.destroy_process_group()
         return
+    # plain one-map-per-launch loop, one bunch at a time (the C++ driver:
+    # the reference's loop over include/vfps.hpp)
+    plain_value, _ = plain_driver(p, 0, 4, False, 1000, 20,
+                                  Ib=float(currents[NB // 2]))
     hbm, peak_kind = peaks()
     # dominant kernel: the fused maps of chain 0 (reads and writes every
     # density cell once: 8 algorithmic bytes per cell)
@@ -653,14 +714,34 @@ def main():
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk.summary(),
         "plain_loop": {"value": plain_value, "unit": "cell-updates/s",
-                       "driver": "Python, one map per launch"},
+                       "driver": "C++ (include/vfps.hpp), one map per "
+                                 "launch, one bunch of the scan"},
         "batched_over_plain": value / plain_value,
     }
     if not args.no_cpu:
         zh = z.data()
         line["cpu_baseline"] = cpu_baseline(p, currents, zh)
-        line["accuracy"] = accuracy_check(snap_low, p, currents, zh,
-                                          args.warmup + args.steps)
+        line["accuracy"] = accuracy_check(batch, start, p, currents, zh,
+                                          os.cpu_count() or 1)
+    if not args.no_configs and world == 1:
+        # the other workloads of the benchmark plan (not the headline)
+        cores = os.cpu_count() or 1
+        t_cfg = time.perf_counter()
+        cfgs = {}
+        for key, fn in (
+                ("plain_256_rotation",
+                 lambda: config_plain_rotation(ctx, hbm)),
+                ("bursting_512", lambda: config_bursting(ctx, stream, hbm)),
+                ("uneven_96", lambda: config_uneven(ctx, stream, hbm, cores)),
+                ("scan_rotation_chain",
+                 lambda: config_scan_rotation(ctx, stream, hbm, p, currents,
+                                              z))):
+            try:
+                cfgs[key] = fn()
+            except Exception as e:   # reported, the headline stands
+                cfgs[key] = {"error": repr(e)[:300]}
+        cfgs["seconds"] = time.perf_counter() - t_cfg
+        line["configs"] = cfgs
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

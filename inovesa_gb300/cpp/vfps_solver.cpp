@@ -9,9 +9,13 @@
 // solver loop.  Usage:
 //     vfps_solver RUNFILE OUTPREFIX
 // writes OUTPREFIX.density (nx*nx float32 after the last step),
-// OUTPREFIX.profile (nx float32) and OUTPREFIX.csr (the CSR power of every
-// step, one per line, when csr = 1).  Exit status 0 on success; errors are
-// printed and give status 1.
+// OUTPREFIX.profile (nx float32), OUTPREFIX.csr (the CSR power of every
+// step, one per line, when csr = 1) and OUTPREFIX.timing ("steps seconds"
+// of the timed steps: the run file's optional "warmup" steps run first,
+// untimed; the device is synchronised before the clock starts and before
+// it stops).  Exit status 0 on success; errors are printed and give status
+// 1.
+#include <chrono>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -157,9 +161,16 @@ int run(const char* runfile, const std::string& prefix)
 
     // the solver loop (src/main.cpp:948-1053)
     const long steps = long(get(p, "steps"));
+    const auto wu = p.find("warmup");
+    const long warmup = wu == p.end() ? 0 : long(wu->second);
     const float fc = float(get(p, "fc"));
     std::vector<float> csr_power;
-    for (long s = 0; s < steps; s++) {
+    auto t0 = std::chrono::steady_clock::now();
+    for (long s = 0; s < warmup + steps; s++) {
+        if (s == warmup) {
+            ctx->synchronize();
+            t0 = std::chrono::steady_clock::now();
+        }
         if (wkm) {
             wkm->update();
         }
@@ -182,6 +193,14 @@ int run(const char* runfile, const std::string& prefix)
             fpm->apply();
         }
         t1->updateXProjection();
+    }
+    ctx->synchronize();
+    const double seconds = std::chrono::duration<double>(
+        std::chrono::steady_clock::now() - t0).count();
+    {
+        std::ofstream out(prefix + ".timing");
+        out.precision(9);
+        out << steps << " " << seconds << "\n";
     }
     write_floats(prefix + ".density", t1->getData());
     write_floats(prefix + ".profile", t1->getProjection(0));

@@ -177,9 +177,11 @@ def csr_impedance_args(p):
                 frev=p["f_rev"], gap=p["gap"] if p["gap"] > 0 else -1.0)
 
 
-def run_file(p, chain=0, it=None, clamp=False, steps=1, csr=False, Ib=None):
+def run_file(p, chain=0, it=None, clamp=False, steps=1, csr=False, Ib=None,
+             warmup=0):
     """The "key = value" run file of the C++ solver driver
-    (inovesa_gb300/cpp/vfps_solver.cpp) for derived parameters p."""
+    (inovesa_gb300/cpp/vfps_solver.cpp) for derived parameters p: `warmup`
+    untimed steps, then `steps` timed ones."""
     o = p["opts"]
     a = p["axes"]
     w = wake_impedance_args(p)
@@ -200,7 +202,7 @@ def run_file(p, chain=0, it=None, clamp=False, steps=1, csr=False, Ib=None):
         f_RF=p["f_RF"], V_eff=p["V_eff"], V0=p["V0"], nslip=len(slip),
         e1=p["e1"], fptype=int(o["FPType"]), fptrack=int(o["FPTrack"]),
         derivation=int(o["derivation"]), fc=p["fc"], csr=int(bool(csr)),
-        steps=int(steps))
+        steps=int(steps), warmup=int(warmup))
     for k, v in enumerate(slip):
         kv["slip%d" % k] = v
     return "".join("%s = %r\n" % (k, float(v)) for k, v in kv.items())

@@ -305,6 +305,62 @@ def fp_apply(data, derivation, idx, w, dtype=np.float64):
     return out
 
 
+
+def fp_particle(mode, n, derivation, idx, w, pos, density=None, e1=0.0,
+                dp=1.0, noise=None):
+    """FokkerPlanckMap::applyTo (src/SM/FokkerPlanckMap.cpp:214-268) for
+    particles pos[k] = (x, y) in mesh units, in float arithmetic as the
+    reference (interpol_t = meshdata_t = float).  Small cases only (a
+    Python loop per particle).
+
+    mode 1 (approximation1): the stencil's mean index displacement at
+      yi = floor(y): y += sum_j (yi - idx_j) w_j, clamped to [1, n-1].
+      The reference bounds yi by n (one row past the table); here yi is
+      bounded by n - 1, which only matters for y >= n - 1.
+    mode 2 (approximation2): the same displacement weighted by the
+      density of bunch 0 at row xi = floor(x): offset = sum_j v_j (idx_j -
+      yi) / sum_j v_j with v_j = f[xi][idx_j] w_j; y += offset, clamped.
+      Particles below the mesh (xi or yi < 0) are left where they are (the
+      reference indexes before the mesh there).
+    mode 3 (stochastic): y -= y e1 + noise[k], the noise drawn from
+      N(0, sqrt(2 e1)/dp) by the caller (the reference draws it from an
+      unseeded generator)."""
+    f32 = np.float32
+    p = np.array(pos, np.float32).reshape(-1, 2).copy()
+    idx = np.asarray(idx, np.uint32).reshape(n, derivation)
+    w = np.asarray(w, np.float32).reshape(n, derivation)
+    lo, hi = f32(1), f32(n - 1)
+    for k in range(p.shape[0]):
+        y = p[k, 1]
+        if mode == 1:
+            yi = min(max(int(np.floor(y)), 0), n - 1)
+            off = f32(0)
+            for j in range(derivation):
+                dy = f32(yi) - f32(idx[yi, j])
+                off = f32(off + f32(dy * w[yi, j]))
+            p[k, 1] = max(lo, min(f32(y + off), hi))
+        elif mode == 2:
+            xi = min(int(np.floor(p[k, 0])), n - 1)
+            yi = min(int(np.floor(y)), n - 1)
+            if xi < 0 or yi < 0:
+                continue
+            d = np.asarray(density, np.float32).reshape(-1, n, n)[0]
+            off = f32(0)
+            charge = f32(0)
+            for j in range(derivation):
+                h = int(idx[yi, j])
+                v = f32(d[xi, h] * w[yi, j])
+                charge = f32(charge + v)
+                off = f32(off + f32(v * f32(h - yi)))
+            with np.errstate(divide="ignore", invalid="ignore"):
+                # no charge under the stencil: NaN, which the clamp below
+                # turns into 1 as std::min/std::max do in the reference
+                off = f32(off / charge)
+            p[k, 1] = max(lo, min(f32(y + off), hi))
+        elif mode == 3:
+            p[k, 1] = f32(y - f32(f32(y * f32(e1)) + f32(noise[k])))
+    return p
+
 # -------------------------------------------------------------- impedance
 def airy(x):
     out = (C.c_double * 4)()

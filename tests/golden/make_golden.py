@@ -1,8 +1,9 @@
 """Extract golden vectors from the reference's unit tests into JSON.
 
-Run once where the Inovesa sources are available:
+Run once where the Inovesa sources are available, with the path of the
+source tree (the directory that holds test/) as the only argument:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <inovesa source tree>
 
 It reads the Boost.Test sources under test/ as text (nothing is compiled or
 run) and writes tests/golden/reference_tests.json with, per test case, the
@@ -229,4 +230,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <inovesa source tree>")
+    main(sys.argv[1])
