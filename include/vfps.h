@@ -426,6 +426,13 @@ VFPS_API int vfps_batch_potential_well(vfps_batch* batch, uint32_t iterations,
 /* kernel launches per solver step (for launch accounting) */
 VFPS_API int vfps_batch_info(const vfps_batch* batch, uint32_t* launches,
                              uint32_t* tile_rows);
+/* No reference counterpart.  Tiles each maps kernel of the batched step
+ * walks, in the order: the fast chain-0 ring kernel (meshes up to 256 rows
+ * with the regular lattice form), the chain-0 ring kernel for the other
+ * meshes up to 256 rows, the 512-row ring kernel, the 1024-row kernel, the
+ * rotation chain's kernel; tiles[count] receives the first count. */
+VFPS_API int vfps_batch_kernel_tiles(const vfps_batch* batch, uint32_t* tiles,
+                                     uint32_t count);
 /* Advance every bunch by nsteps solver steps launched one kernel at a time
  * with CUDA events between the kernels, and return the mean duration per
  * step of each kernel in ms[3] (wake, chain-0 maps, chain-1 maps; 0 for a

@@ -157,6 +157,7 @@ SIGNATURES = {
                            C.c_uint32],
     "vfps_batch_get_csr": [P, FP, U64P],
     "vfps_batch_info": [P, U32P, U32P],
+    "vfps_batch_kernel_tiles": [P, U32P, u32],
     "vfps_batch_kernel_times": [P, u32, FP],
     "vfps_charge_noalloc": [P, P, u32, u32, flt, DP],
     "vfps_batch_set_wake_mode": [P, i32],

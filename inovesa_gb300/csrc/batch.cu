@@ -36,12 +36,16 @@
 #include "vfps_internal.cuh"
 
 #include "batch_kernels.cuh"
+#include "ring_fast.cuh"
 #include "wake_tc.cuh"
 
 using vfps::DevBuf;
 
 // ================================================================== host
-enum { TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_COUNT = 4 };
+enum {
+    TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_RINGF = 4,
+    TL_COUNT = 5
+};
 constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel, G = 2
 constexpr int RING4_N = 512;      // the mesh of the ring kernel, G = 4
 constexpr int RTHREADS4 = 256;    // its CTA: 8 warps, one row each
@@ -52,8 +56,10 @@ struct vfps_batch {
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    // tile lists: TL_RING (chain 0, n <= 256), TL_RING4 (chain 0, n = 512),
-    // TL_ROT (chain 1), TL_WIDE (chain 0, n = 1024)
+    // tile lists: TL_RINGF (chain 0, n <= 256, regular lattices: the fast
+    // ring kernel), TL_RING (the other chain-0 meshes up to 256 rows),
+    // TL_RING4 (chain 0, n = 512), TL_ROT (chain 1), TL_WIDE (chain 0,
+    // n = 1024)
     std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
     uint32_t max_n = 0;
@@ -67,6 +73,7 @@ struct vfps_batch {
     DevBuf<float> dens[2], prof[2];
     DevBuf<float> wake, factor;
     DevBuf<RowInfo> rinfo;     // chain-0 y-kick stencils of every row
+    DevBuf<RowInfo7> rinfo7;   // the same as one 7-tap stencil (F_Y7)
     DevBuf<double> filling;
     // k_bwake's CTAs: (bunch, first row) of each block of rows
     DevBuf<uint2> wblk;
@@ -80,6 +87,8 @@ struct vfps_batch {
     unsigned gridR = 0;        // persistent CTAs of k_bmaps0
     SmemR layoutR4{};          // the same for the 512-row ring kernel
     unsigned gridR4 = 0;
+    SmemR layoutRF{};          // the same for the fast ring kernel
+    unsigned gridRF = 0;
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
@@ -202,7 +211,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     }
     k_bwake<<<b->nwblk, THREADS, wsm, st>>>(
         b->bd.p, b->wblk.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p,
-        b->wake.p, b->rinfo.p, b->factor.p, b->filling.p, b->tickets.p,
+        b->wake.p, b->rinfo.p, b->rinfo7.p, b->factor.p, b->filling.p,
+        b->tickets.p,
         b->beams.p, b->members.p,
         CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
                b->csr_every, b->csr_cap, b->nb, b->csrpart.p, b->csrdone.p},
@@ -223,7 +233,7 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     // that each fills the SMs the others leave free (no kernel's tail
     // idles the GPU); sequential when the kernels are timed one by one
     int classes = 0;
-    for (int c : {TL_RING, TL_RING4, TL_WIDE, TL_ROT}) {
+    for (int c : {TL_RINGF, TL_RING, TL_RING4, TL_WIDE, TL_ROT}) {
         classes += b->htiles[c].empty() ? 0 : 1;
     }
     const bool forked = !ev && classes > 1;
@@ -239,7 +249,7 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
         return s;
     };
     auto ring_launch = [&](auto kernel, int list, unsigned grid, int threads,
-                           const SmemR& layout) {
+                           const SmemR& layout, auto rinfo) {
         if (b->htiles[list].empty()) {
             return;
         }
@@ -255,14 +265,16 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             &c, kernel, (const BDev*)b->bd.p, (const Tile*)b->tiles[list].p,
             static_cast<uint32_t>(b->htiles[list].size()),
             (const float*)b->tabs.p, (const float*)b->dwt.p,
-            (const RowInfo*)b->rinfo.p, (const float*)b->dens[from].p,
+            rinfo, (const float*)b->dens[from].p,
             b->dens[to].p, b->prof[to].p, b->ctx->d_status, layout));
         VFPS_LAUNCHED();
     };
+    ring_launch(k_bmaps0f<RTHREADS>, TL_RINGF, b->gridRF, RTHREADS,
+                b->layoutRF, (const RowInfo7*)b->rinfo7.p);
     ring_launch(k_bmaps0<2, RTHREADS>, TL_RING, b->gridR, RTHREADS,
-                b->layoutR);
+                b->layoutR, (const RowInfo*)b->rinfo.p);
     ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
-                b->layoutR4);
+                b->layoutR4, (const RowInfo*)b->rinfo.p);
     if (!b->htiles[TL_WIDE].empty()) {
         k_bmaps0w<<<b->grid0, THREADS, b->smem[TL_WIDE], next_stream()>>>(
             b->bd.p, b->tiles[TL_WIDE].p,
@@ -316,16 +328,17 @@ void build_tiles(vfps_batch* b, int tile_cells)
     int max_rows = 0;
     // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
-    int ring_rows = 0, ring_n = 0, ring4_rows = 0;
+    int ring_rows = 0, ring_n = 0, ring4_rows = 0, ringf_rows = 0,
+        ringf_n = 0;
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
         const int c = B.chain == 1 ? TL_ROT
-                      : (n <= RING_MAX_N ? TL_RING
-                                         : (n == RING4_N ? TL_RING4
-                                                         : TL_WIDE));
+                      : (n <= RING_MAX_N
+                             ? ((B.flags & F_Y7) ? TL_RINGF : TL_RING)
+                             : (n == RING4_N ? TL_RING4 : TL_WIDE));
         int tx = std::max(4, tile_cells / n);
-        if (c == TL_RING || c == TL_RING4) {
+        if (c == TL_RING || c == TL_RING4 || c == TL_RINGF) {
             // the ring holds two tiles with their halos: at most 32 staged
             // rows per tile keeps it at 64 slots or fewer
             tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
@@ -340,6 +353,9 @@ void build_tiles(vfps_batch* b, int tile_cells)
         if (c == TL_RING) {
             ring_rows = std::max(ring_rows, nr);
             ring_n = std::max(ring_n, n);
+        } else if (c == TL_RINGF) {
+            ringf_rows = std::max(ringf_rows, nr);
+            ringf_n = std::max(ringf_n, n);
         } else if (c == TL_RING4) {
             ring4_rows = std::max(ring4_rows, nr);
         } else if (c == TL_WIDE) {
@@ -359,26 +375,35 @@ void build_tiles(vfps_batch* b, int tile_cells)
         o = align16(o + bytes);
     };
     // the ring holds the staged rows of two tiles with their halos
-    auto ring_layout = [&](SmemR& L, int rows, int n) {
+    auto ring_layout = [&](SmemR& L, int rows, int n, size_t rec) {
         const int rb = 2 * rows;
         L.rb = static_cast<uint32_t>(rb);
         L.rs = static_cast<uint32_t>(astride0(n));
         o = 0;
         take(&L.ring, size_t(rb) * L.rs * 4);
-        take(&L.s, size_t(rows) * sizeof(RowInfo));
+        take(&L.s, size_t(rows) * rec);
         take(&L.tab, size_t(10) * n * 4);
         take(&L.bar, 3 * sizeof(uint64_t));
         L.total = static_cast<uint32_t>(o);
         return o;
     };
+    if (!b->htiles[TL_RINGF].empty()) {
+        b->smem[TL_RINGF] = ring_layout(b->layoutRF, ringf_rows, ringf_n,
+                                        sizeof(RowInfo7));
+        b->gridRF = persistent_grid(b, k_bmaps0f<RTHREADS>, RTHREADS,
+                                    b->smem[TL_RINGF],
+                                    b->htiles[TL_RINGF].size());
+    }
     if (!b->htiles[TL_RING].empty()) {
-        b->smem[TL_RING] = ring_layout(b->layoutR, ring_rows, ring_n);
+        b->smem[TL_RING] = ring_layout(b->layoutR, ring_rows, ring_n,
+                                       sizeof(RowInfo));
         b->gridR = persistent_grid(b, k_bmaps0<2, RTHREADS>, RTHREADS,
                                    b->smem[TL_RING],
                                    b->htiles[TL_RING].size());
     }
     if (!b->htiles[TL_RING4].empty()) {
-        b->smem[TL_RING4] = ring_layout(b->layoutR4, ring4_rows, RING4_N);
+        b->smem[TL_RING4] = ring_layout(b->layoutR4, ring4_rows, RING4_N,
+                                        sizeof(RowInfo));
         b->gridR4 = persistent_grid(b, k_bmaps0<4, RTHREADS4>, RTHREADS4,
                                     b->smem[TL_RING4],
                                     b->htiles[TL_RING4].size());
@@ -418,6 +443,10 @@ void upload_tiles(vfps_batch* b)
 {
     VFPS_REQUIRE(tiles_fit(b),
                  "tile of the largest mesh does not fit in shared memory");
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADS>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_RINGF], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<2, RTHREADS>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
@@ -696,6 +725,39 @@ std::vector<float> fp_weights(const vfps::Axis& ay, float e1, int fptype,
     return w5;
 }
 
+// The lattice forms k_bmaps0f takes: every aligned group of 4 energy
+// columns has one drift shift (its lanes load one window row per group),
+// and the Fokker-Planck stencils of the lower half of the energy columns
+// reach offsets -2..1 only, those of the upper half -1..2 only (4 taps),
+// except the last column of the lower half, which may reach -2..2 (the
+// reference starts its upper stencils at the truncated centre, which is
+// that column on a mesh centred on the reference energy)
+bool fast_ring_ok(const std::vector<RowStencil>& dr,
+                  const std::vector<float>& w5, uint32_t n)
+{
+    for (uint32_t y = 0; y < n; y += 4) {
+        for (uint32_t c = 1; c < 4; c++) {
+            if (dr[y + c].shift0 != dr[y].shift0) {
+                return false;
+            }
+        }
+    }
+    for (uint32_t y = 0; y < n; y++) {
+        if (y + 1 != n / 2 && w5[size_t(y) * 5 + (y < n / 2 ? 4 : 0)] != 0.f) {
+            return false;
+        }
+    }
+    return true;
+}
+
+// VFPS_RING_KERNEL=classic keeps every chain-0 mesh up to 256 rows on
+// k_bmaps0 (the two kernels side by side in tests and profiles)
+bool fast_ring_off()
+{
+    const char* v = std::getenv("VFPS_RING_KERNEL");
+    return v && std::string(v) == "classic";
+}
+
 }  // namespace
 
 extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
@@ -885,6 +947,10 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                     for (uint32_t y = 0; y < n; y++) {
                         tab.push_back(w5[size_t(y) * 5 + o]);
                     }
+                }
+                if (n <= RING_MAX_N && fast_ring_ok(dr, w5, n)
+                    && !fast_ring_off()) {
+                    B.flags |= F_Y7;
                 }
                 // bunches of a scan share these tables: one copy each, so
                 // that a ring kernel's CTA stages a shared one only once
@@ -1078,6 +1144,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         b->wake.alloc(b->rows);
         b->rinfo.alloc(b->rows);
         VFPS_CUDA(cudaMemsetAsync(b->rinfo.p, 0, b->rinfo.bytes(), st));
+        b->rinfo7.alloc(b->rows);
+        VFPS_CUDA(cudaMemsetAsync(b->rinfo7.p, 0, b->rinfo7.bytes(), st));
         VFPS_CUDA(cudaMemsetAsync(b->wake.p, 0, b->wake.bytes(), st));
         b->factor.alloc(nb);
         b->filling.alloc(nb);
@@ -1424,6 +1492,19 @@ extern "C" int vfps_batch_info(const vfps_batch* b, uint32_t* launches,
     }
     if (tile_rows) {
         *tile_rows = static_cast<uint32_t>(b->tile_rows);
+    }
+    return VFPS_OK;
+}
+
+extern "C" int vfps_batch_kernel_tiles(const vfps_batch* b, uint32_t* tiles,
+                                       uint32_t count)
+{
+    if (!b || (count && !tiles)) {
+        return VFPS_ERR_INVALID_ARGUMENT;
+    }
+    const int order[] = {TL_RINGF, TL_RING, TL_RING4, TL_WIDE, TL_ROT};
+    for (uint32_t k = 0; k < count && k < 5; k++) {
+        tiles[k] = static_cast<uint32_t>(b->htiles[order[k]].size());
     }
     return VFPS_OK;
 }

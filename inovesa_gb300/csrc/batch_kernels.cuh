@@ -105,7 +105,22 @@ struct __align__(16) RowInfo {
     int pad[2];
 };
 
-enum { F_WAKE = 1, F_FP = 2, F_CLAMP = 4 };
+// per mesh row of chain 0 for the fast ring kernel (k_bmaps0f): both
+// y-kicks as one 7-tap stencil, out[y] = sum_k c[k] t1[y + s + k], with
+// s = sa + sb and c[k] = sum_{i+j=k} a[i] b[j] (the wake kick's weights a,
+// times the renormalisation factor, then the RF kick's b).  The same
+// product of the two kicks except at the energy edges, where the
+// reference drops the first kick's values that land off the mesh before
+// the second kick (the composite keeps them: they carry the density of
+// the outermost cells, about 1e-8 of the peak on a +-6 sigma mesh)
+struct __align__(16) RowInfo7 {
+    int s;
+    float c[7];
+};
+static_assert(sizeof(RowInfo7) == 32, "two 16-byte loads per row");
+
+// F_Y7: the bunch runs on k_bmaps0f (k_bwake writes RowInfo7 records)
+enum { F_WAKE = 1, F_FP = 2, F_CLAMP = 4, F_Y7 = 8 };
 enum { TAB_WS = 0, TAB_Q = 1, TAB_P = 2, TAB_COUNT = 3 };
 enum { ST_RF = 0, ST_DRIFT = 1, ST_COUNT = 2 };
 
@@ -311,7 +326,8 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
         const float* __restrict__ tabs,
         const float* __restrict__ wt, const RowStencil* __restrict__ st,
         const float* __restrict__ pin, float* __restrict__ wake,
-        RowInfo* __restrict__ rinfo, float* __restrict__ factor,
+        RowInfo* __restrict__ rinfo, RowInfo7* __restrict__ rinfo7,
+        float* __restrict__ factor,
         double* __restrict__ filling, unsigned long long* __restrict__ tickets,
         const BeamDev* __restrict__ beams,
         const uint32_t* __restrict__ members, CsrRec csr,
@@ -450,6 +466,28 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
             sa.w[1] = sa.w[2] = sa.w[3] = 0.f;
         }
         const RowStencil sb = xl == x0 ? sb0 : rf[x];
+        if (B.flags & F_Y7) {
+            RowInfo7 r7;
+            r7.s = sa.shift0 + sb.shift0;
+            float a[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                a[j] = sa.w[j] * fac;
+            }
+#pragma unroll
+            for (int k = 0; k < 7; k++) {
+                float c = 0.f;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    if (k - i >= 0 && k - i < 4) {
+                        c = fmaf(a[i], sb.w[k - i], c);
+                    }
+                }
+                r7.c[k] = c;
+            }
+            rinfo7[B.prof_off + x] = r7;
+            continue;
+        }
         RowInfo ri;
         ri.s = sa.shift0 + sb.shift0;
         ri.sb = sb.shift0;
@@ -1141,12 +1179,22 @@ k_bmaps0w(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         }
 
         // wait for this tile's rows (bounded: a wait that runs out flags
-        // VFPS_ERR_TIMEOUT and keeps waiting a bounded time more)
+        // VFPS_ERR_TIMEOUT and keeps waiting a bounded time more).  A CTA
+        // whose wait ran out stops walking its tiles: the next tile's
+        // copies, already issued, get one bounded wait, and the kernel
+        // reports the timeout after about one wait limit
         if (!mbar_wait_bounded(&bar[cur], (k >> 1) & 1, WAIT_NS)) {
             bad = 1;
             mbar_wait_bounded(&bar[cur], (k >> 1) & 1, WAIT_NS);
         }
-        __syncthreads();
+        if (__syncthreads_or(bad)) {
+            bad = 1;
+            if (nxt < t_end) {
+                mbar_wait_bounded(&bar[cur ^ 1], ((k + 1) >> 1) & 1,
+                                  WAIT_NS);
+            }
+            break;
+        }
         if (threadIdx.x == 0 && nxt < t_end) {
             const Tile tn = tiles[nxt];
             note_slots(bd[tn.bunch], tn, &pads[2 * (cur ^ 1)]);
@@ -1402,12 +1450,13 @@ struct RingMap {
 // barrier with the byte count of both parts first (lane 0); the stencils
 // part may follow later, the barrier's phase completes when both have
 // landed.
+template <typename Rec>
 __device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
                                            const RingMap& m, float* ring,
                                            int rb, int rs,
                                            const float* __restrict__ din,
-                                           const RowInfo* __restrict__ rinfo,
-                                           RowInfo* S, uint64_t* bar,
+                                           const Rec* __restrict__ rinfo,
+                                           Rec* S, uint64_t* bar,
                                            bool rows = true,
                                            bool stencils = true)
 {
@@ -1416,7 +1465,7 @@ __device__ __forceinline__ void issue_rows(const BDev& B, int lo, int hi,
     // all beyond the mesh end (the previous tile's halo reached past it)
     const int a = max(lo, 0), e = max(min(hi, n), a);
     const uint32_t row_bytes = uint32_t(n) * 4u;
-    const uint32_t ri_bytes = uint32_t(e - a) * uint32_t(sizeof(RowInfo));
+    const uint32_t ri_bytes = uint32_t(e - a) * uint32_t(sizeof(Rec));
     const int lane = threadIdx.x & 31;
     if (lane == 0) {
         if (rows) {
@@ -1883,9 +1932,20 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 }
             }
         }
-        // the in-place writes precede later bulk copies into these slots
+        // the in-place writes precede later bulk copies into these slots.
+        // A wait of this CTA that ran out (here or on the tables) ends its
+        // walk: no further copies are issued, the one of the tables still
+        // in flight gets one more bounded wait, and the kernel reports
+        // VFPS_ERR_TIMEOUT after about one wait limit instead of one per
+        // remaining tile
         fence_proxy_async();
-        __syncthreads();
+        if (__syncthreads_or(bad)) {
+            bad = 1;
+            if (tab_wait) {
+                mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS);
+            }
+            break;
+        }
 
         // stage the next tile's new rows: their slots hold no row that this
         // tile still reads (the ring holds two tiles with their halos)

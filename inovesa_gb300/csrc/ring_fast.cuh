@@ -1,0 +1,477 @@
+// k_bmaps0f: chain 0 (the reference's loop, src/main.cpp:1034-1044:
+// wake kick, RF kick, drift, Fokker-Planck) for meshes of 64..256 rows
+// whose lattice has the regular form of the benchmark's scans (checked on
+// the host, fast_ring_ok): every aligned group of 4 energy columns has one
+// drift shift, and the Fokker-Planck stencil of the lower half of the
+// energy axis spans offsets -2..1, that of the upper half -1..2 (the
+// cubic stencil of a mesh centred on the reference energy, whose last
+// lower column may take the upper form and reach -2..2; two-sided
+// stencils and no Fokker-Planck fit too).  Other lattices run on k_bmaps0.
+//
+// Included by batch.cu after batch_kernels.cuh (shares its ring, tiles and
+// bulk-copy helpers).  Per tile of rows, as k_bmaps0:
+//  stage 1  both y-kicks of the tile's new staged rows as one 7-tap
+//           stencil (RowInfo7), in place in the ring: a row's shift is
+//           the same for all its lanes, so the window alignment and the
+//           bounds test are warp-uniform branches;
+//  stage 2  each segment of n/8 lanes walks a contiguous run of the
+//           tile's output rows with a sliding window of 4 staged rows per
+//           group of 4 columns in registers (one new row per output row),
+//           the drift weights in registers for the whole tile, the drift
+//           in packed FP32, Fokker-Planck with 4 taps (neighbour columns
+//           by shuffles), the new row to HBM and its Simpson sum; the row
+//           sums of 4 output rows leave in one reduce-scatter.
+#pragma once
+
+namespace {
+
+// 4 outputs y..y+3 of the composite y-kick from the 16-byte aligned
+// window src (AL: offset of column y + s in it)
+template <int AL>
+__device__ __forceinline__ float4 ykick7(const float* src, const float (&c)[7])
+{
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float v[16];
+    const float4 v0 = s4[0], v1 = s4[1], v2 = s4[2];
+    v[0] = v0.x; v[1] = v0.y; v[2] = v0.z; v[3] = v0.w;
+    v[4] = v1.x; v[5] = v1.y; v[6] = v1.z; v[7] = v1.w;
+    v[8] = v2.x; v[9] = v2.y; v[10] = v2.z; v[11] = v2.w;
+    if (AL == 3) {
+        const float4 v3 = s4[3];
+        v[12] = v3.x; v[13] = v3.y; v[14] = v3.z; v[15] = v3.w;
+    } else {
+        v[12] = v[13] = v[14] = v[15] = 0.f;
+    }
+    float o[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float a = c[0] * v[AL + q];
+#pragma unroll
+        for (int k = 1; k < 7; k++) {
+            a = fmaf(c[k], v[AL + q + k], a);
+        }
+        o[q] = a;
+    }
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// the same with every read bounds-checked against the staged row [0, as)
+__device__ __forceinline__ float4 ykick7_checked(const float* row, int start,
+                                                 int as, const float (&c)[7])
+{
+    float v[10];
+#pragma unroll
+    for (int q = 0; q < 10; q++) {
+        const int p = start + q;
+        v[q] = (p >= 0 && p < as) ? row[p] : 0.f;
+    }
+    float o[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        float a = c[0] * v[q];
+#pragma unroll
+        for (int k = 1; k < 7; k++) {
+            a = fmaf(c[k], v[q + k], a);
+        }
+        o[q] = a;
+    }
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// drift x-kick of 4 columns: tap j of the output reads window row r[j]
+// (packed FP32: two columns per instruction, each component rounded like
+// fmaf / a plain product)
+__device__ __forceinline__ float4 drift4(const float4& r0, const float4& r1,
+                                         const float4& r2, const float4& r3,
+                                         const float4 (&w)[4])
+{
+    float2 lo = __fmul2_rn(make_float2(w[0].x, w[0].y),
+                           make_float2(r0.x, r0.y));
+    float2 hi = __fmul2_rn(make_float2(w[0].z, w[0].w),
+                           make_float2(r0.z, r0.w));
+    lo = __ffma2_rn(make_float2(w[1].x, w[1].y), make_float2(r1.x, r1.y), lo);
+    hi = __ffma2_rn(make_float2(w[1].z, w[1].w), make_float2(r1.z, r1.w), hi);
+    lo = __ffma2_rn(make_float2(w[2].x, w[2].y), make_float2(r2.x, r2.y), lo);
+    hi = __ffma2_rn(make_float2(w[2].z, w[2].w), make_float2(r2.z, r2.w), hi);
+    lo = __ffma2_rn(make_float2(w[3].x, w[3].y), make_float2(r3.x, r3.y), lo);
+    hi = __ffma2_rn(make_float2(w[3].z, w[3].w), make_float2(r3.z, r3.w), hi);
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+// Fokker-Planck of 4 columns with 4 taps: out[c] = sum_o F_o[c] w[c + o]
+// (w: the 7 drift values the taps reach, F_o: weight planes)
+__device__ __forceinline__ float4 fp4(const float (&w)[7], const float4& f0,
+                                      const float4& f1, const float4& f2,
+                                      const float4& f3)
+{
+    const float a0[4] = {f0.x, f0.y, f0.z, f0.w};
+    const float a1[4] = {f1.x, f1.y, f1.z, f1.w};
+    const float a2[4] = {f2.x, f2.y, f2.z, f2.w};
+    const float a3[4] = {f3.x, f3.y, f3.z, f3.w};
+    float o[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float v = a0[c] * w[c];
+        v = fmaf(a1[c], w[c + 1], v);
+        v = fmaf(a2[c], w[c + 2], v);
+        v = fmaf(a3[c], w[c + 3], v);
+        o[c] = v;
+    }
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 3)
+k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
+          uint32_t ntiles, const float* __restrict__ tabs,
+          const float* __restrict__ dwt, const RowInfo7* __restrict__ rinfo,
+          const float* __restrict__ din, float* __restrict__ dout,
+          float* __restrict__ pout, int* __restrict__ status, SmemR L)
+{
+    extern __shared__ float4 smem4[];
+    char* base = reinterpret_cast<char*>(smem4);
+    float* ring = reinterpret_cast<float*>(base + L.ring);
+    RowInfo7* S = reinterpret_cast<RowInfo7*>(base + L.s);
+    float* T = reinterpret_cast<float*>(base + L.tab);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
+    const int rb = int(L.rb), rs = int(L.rs);
+    const int ring_floats = rb * rs;
+    const int lane = threadIdx.x & 31;
+
+    // the ring starts zero: slots are written only in [APAD, n + APAD)
+    {
+        float4* r4 = reinterpret_cast<float4*>(ring);
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int i = threadIdx.x; i < ring_floats / 4; i += NT) {
+            r4[i] = z;
+        }
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_init(&bar[2], 1);
+        mbar_fence_init();
+    }
+    fence_proxy_async();
+    __syncthreads();
+
+    // a contiguous chunk of the tile list per CTA (chunks differ by at
+    // most one tile)
+    const uint32_t t_begin = uint32_t(uint64_t(blockIdx.x) * ntiles
+                                      / gridDim.x);
+    const uint32_t t_end = uint32_t(uint64_t(blockIdx.x + 1) * ntiles
+                                    / gridDim.x);
+
+    RingMap mc{0}, mn{0};
+    int lo_c = 0, hi_c = 0, lo_n = 0, hi_n = 0;
+    int front = 0;
+    uint32_t tab_off = 0xffffffffu, tab_ph = 0;
+    bool tab_wait = false;
+    auto load_tab = [&](const BDev& Bt) {
+        const uint32_t bytes = 10u * Bt.n * 4u;
+        if (threadIdx.x == 0) {
+            fence_proxy_async();
+            mbar_arrive_expect_tx(&bar[2], bytes);
+            tma_load_1d(T, dwt + Bt.dw_off, bytes, &bar[2]);
+        }
+        tab_off = Bt.dw_off;
+        tab_wait = true;
+    };
+    if (t_begin < t_end) {
+        const Tile t = tiles[t_begin];
+        const BDev B = bd[t.bunch];
+        load_tab(B);
+        lo_c = int(t.x0) - B.halo_lo;
+        hi_c = int(t.x0 + t.rows) + B.halo_hi;
+        mc = RingMap::at(lo_c, 0);
+        front = hi_c - lo_c;
+        // the first tile's density rows while the stencil kernel runs
+        if (threadIdx.x < 32) {
+            issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, rinfo, S,
+                       &bar[0], true, false);
+        }
+    }
+    // this step's stencils are complete
+    pdl_wait();
+    if (t_begin < t_end && threadIdx.x < 32) {
+        const BDev B = bd[tiles[t_begin].bunch];
+        issue_rows(B, lo_c, hi_c, mc, ring, rb, rs, din, rinfo, S, &bar[0],
+                   false, true);
+    }
+    int bad = 0;
+    for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
+        const Tile t = tiles[tid];
+        const BDev B = bd[t.bunch];
+        const int n = int(B.n);
+        const int x0 = int(t.x0);
+        const int rows = int(t.rows);
+        const int seg = n >> 3;              // lanes per row
+        const int l = threadIdx.x & (seg - 1);
+        const int rl = threadIdx.x / seg;    // segment
+        const int rp = NT / seg;             // segments
+        const int as = astride0(n);
+        const int yA = 4 * l, yB = (n >> 1) + 4 * l;
+
+        // stage 1: both y-kicks of the new rows, in place
+        {
+            const int m = hi_c - lo_c;
+            if (!mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, WAIT_NS)) {
+                bad = 1;
+                mbar_wait_bounded(&bar[k & 1], (k >> 1) & 1, WAIT_NS);
+            }
+            const unsigned rmask = seg == 32 ? 0xffffffffu
+                : (((1u << seg) - 1u) << (lane & ~(seg - 1)));
+            const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int i = rl; i < m; i += rp) {
+                const int x = lo_c + i;
+                float* row = ring + size_t(mc.slot(x, rb)) * rs;
+                // zeros right of the row: the slot may have held a longer
+                // row of another bunch
+                if (n + 2 * APAD + 16 < rs) {
+                    for (int j = l; j < (APAD + 16) / 4; j += seg) {
+                        reinterpret_cast<float4*>(row + APAD + n)[j] = z;
+                    }
+                }
+                if (unsigned(x) < unsigned(n)) {
+                    const float4 q0 = reinterpret_cast<const float4*>(S + i)[0];
+                    const float4 q1 = reinterpret_cast<const float4*>(S + i)[1];
+                    const int s = __float_as_int(q0.x);
+                    const float c[7] = {q0.y, q0.z, q0.w, q1.x, q1.y, q1.z,
+                                        q1.w};
+                    float4 oA, oB;
+                    // the window of every lane inside the staged row: the
+                    // lowest starts at APAD + s, the highest ends 16 floats
+                    // after its aligned start APAD + n - 4 + (s & ~3)
+                    if (s >= -APAD && s <= APAD + 7) {
+                        const float* wa = row + APAD + (s & ~3) + yA;
+                        const float* wb = row + APAD + (s & ~3) + yB;
+                        switch (s & 3) {
+                        case 0:
+                            oA = ykick7<0>(wa, c);
+                            oB = ykick7<0>(wb, c);
+                            break;
+                        case 1:
+                            oA = ykick7<1>(wa, c);
+                            oB = ykick7<1>(wb, c);
+                            break;
+                        case 2:
+                            oA = ykick7<2>(wa, c);
+                            oB = ykick7<2>(wb, c);
+                            break;
+                        default:
+                            oA = ykick7<3>(wa, c);
+                            oB = ykick7<3>(wb, c);
+                            break;
+                        }
+                    } else {
+                        oA = ykick7_checked(row, APAD + yA + s, as, c);
+                        oB = ykick7_checked(row, APAD + yB + s, as, c);
+                    }
+                    __syncwarp(rmask);
+                    *reinterpret_cast<float4*>(row + APAD + yA) = oA;
+                    *reinterpret_cast<float4*>(row + APAD + yB) = oB;
+                } else {
+                    *reinterpret_cast<float4*>(row + APAD + yA) = z;
+                    *reinterpret_cast<float4*>(row + APAD + yB) = z;
+                }
+            }
+        }
+        // the in-place writes precede later bulk copies into these slots.
+        // A wait that ran out (here or on the tables) ends the CTA's walk:
+        // no further copies are issued, the tables' copy still in flight
+        // gets one more bounded wait, and the kernel reports
+        // VFPS_ERR_TIMEOUT after about one wait limit
+        fence_proxy_async();
+        if (__syncthreads_or(bad)) {
+            bad = 1;
+            if (tab_wait) {
+                mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS);
+            }
+            break;
+        }
+
+        // stage the next tile's new rows: their slots hold no row that this
+        // tile still reads (the ring holds two tiles with their halos)
+        if (tid + 1 < t_end) {
+            const Tile tn = tiles[tid + 1];
+            const BDev Bn = bd[tn.bunch];
+            const bool cont = tn.bunch == t.bunch
+                              && int(tn.x0) == x0 + rows;
+            hi_n = int(tn.x0 + tn.rows) + Bn.halo_hi;
+            const int xr = int(tn.x0) - Bn.halo_lo;
+            if (cont) {
+                mn = RingMap::at(xr, mc.slot(xr, rb));
+                lo_n = hi_c;
+            } else {
+                lo_n = xr;
+                mn = RingMap::at(xr, front);
+            }
+            front = mn.slot(hi_n, rb);
+            if (threadIdx.x < 32) {
+                issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo, S,
+                           &bar[(k + 1) & 1]);
+            }
+        }
+
+        // this tile's drift and Fokker-Planck planes in T
+        if (B.dw_off != tab_off) {
+            load_tab(B);
+        }
+        if (tab_wait) {
+            if (!mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS)) {
+                bad = 1;
+                mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS);
+            }
+            tab_ph ^= 1u;
+            tab_wait = false;
+        }
+
+        // stage 2: drift, Fokker-Planck, new rows, projections.  Segment rl
+        // walks output rows [ra, ra + per) of the tile in steps of 4 (every
+        // segment makes the same number of steps, so the shuffles see whole
+        // warps; rows past the tile are computed and dropped)
+        {
+            const float* W = T;             // drift weights [4][n], shift [n]
+            const float* F = T + 5 * n;     // Fokker-Planck planes [5][n]
+            const float h03 = tabs[B.tab_off + TAB_WS * n];
+            const int shA = __float_as_int(W[4 * n + yA]);
+            const int shB = __float_as_int(W[4 * n + yB]);
+            float4 wA[4], wB[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                wA[j] = *reinterpret_cast<const float4*>(W + j * n + yA);
+                wB[j] = *reinterpret_cast<const float4*>(W + j * n + yB);
+            }
+            // the Fokker-Planck weights (plane o, column y); the compiler
+            // keeps them in registers across the rows
+            auto fw = [&](int o, int y) {
+                return *reinterpret_cast<const float4*>(F + o * n + y);
+            };
+            const int per = (rows + rp - 1) / rp;
+            const int ra = rl * per;
+            const int xend = x0 + min(rows, ra + per);
+            // window row offsets in the ring (floats), advanced by one slot
+            // per output row (segments past the tile's rows start further
+            // on: reduced modulo the ring)
+            auto slot0 = [&](int x) {
+                int q = (x + mc.off) % rb;
+                return q < 0 ? q + rb : q;
+            };
+            int oA = slot0(x0 + ra + shA) * rs + APAD + yA;
+            int oB = slot0(x0 + ra + shB) * rs + APAD + yB;
+            auto next = [&](int& o) {
+                o += rs;
+                o -= o >= ring_floats ? ring_floats : 0;
+            };
+            float4 a0, a1, a2, a3, b0, b1, b2, b3;
+            a0 = *reinterpret_cast<const float4*>(ring + oA);
+            b0 = *reinterpret_cast<const float4*>(ring + oB);
+            next(oA);
+            next(oB);
+            a1 = *reinterpret_cast<const float4*>(ring + oA);
+            b1 = *reinterpret_cast<const float4*>(ring + oB);
+            next(oA);
+            next(oB);
+            a2 = *reinterpret_cast<const float4*>(ring + oA);
+            b2 = *reinterpret_cast<const float4*>(ring + oB);
+            next(oA);
+            next(oB);
+            const float f4a = F[4 * n + yA + 3];
+            const int lp = (l + 1) & (seg - 1), lm = (l + seg - 1) & (seg - 1);
+            const bool first = l == 0, last = l == seg - 1;
+            const int hs = seg >> 1, qs = seg >> 2;
+            float* obase = dout + B.dens_off;
+            // one output row X from the window rows r0..r3 of each group
+            // (the newest, r3, loaded here): its Simpson-weighted row sum
+            // (in units of h03) is returned
+            auto one = [&](int X, const float4& r0, const float4& r1,
+                           const float4& r2, float4& r3, const float4& s0,
+                           const float4& s1, const float4& s2, float4& s3) {
+                r3 = *reinterpret_cast<const float4*>(ring + oA);
+                s3 = *reinterpret_cast<const float4*>(ring + oB);
+                next(oA);
+                next(oB);
+                const float4 dA = drift4(r0, r1, r2, r3, wA);
+                const float4 dB = drift4(s0, s1, s2, s3, wB);
+                // neighbour columns: A's left (lane l-1's A2, A3) and right
+                // (lane l+1's A0; the last lane takes lane 0's B0), B's
+                // left (lane l-1's B3; lane 0 takes the last lane's A3)
+                // and right (lane l+1's B0, B1).  Beyond the mesh edges the
+                // wrapped values meet zero weights (rows 0, 1, n-2, n-1 of
+                // the Fokker-Planck stencil are zero)
+                const float aL2 = __shfl_sync(0xffffffffu, dA.z, lm, seg);
+                const float aL3 = __shfl_sync(0xffffffffu, dA.w, lm, seg);
+                const float aR0 = __shfl_sync(0xffffffffu, dA.x, lp, seg);
+                const float bL3 = __shfl_sync(0xffffffffu, dB.w, lm, seg);
+                const float bR0 = __shfl_sync(0xffffffffu, dB.x, lp, seg);
+                const float bR1 = __shfl_sync(0xffffffffu, dB.y, lp, seg);
+                const float wa[7] = {aL2, aL3, dA.x, dA.y, dA.z, dA.w,
+                                     last ? bR0 : aR0};
+                const float wb[7] = {first ? aL3 : bL3, dB.x, dB.y, dB.z,
+                                     dB.w, bR0, bR1};
+                // lower half: offsets -2..1 (planes 0..3); upper half:
+                // -1..2 (planes 1..4)
+                float4 fA = fp4(wa, fw(0, yA), fw(1, yA), fw(2, yA),
+                                fw(3, yA));
+                // offset +2 of the lower half's columns: zero but in its
+                // last column (n/2 - 1, the last lane's 4th), whose +2
+                // neighbour n/2 + 1 is lane 0's B1 (bR1 there; elsewhere
+                // bR1 meets the zero weight)
+                fA.w = fmaf(f4a, bR1, fA.w);
+                const float4 fB = fp4(wb, fw(1, yB), fw(2, yB), fw(3, yB),
+                                      fw(4, yB));
+                if (X < xend) {
+                    float* o = obase + size_t(X) * n;
+                    *reinterpret_cast<float4*>(o + yA) = fA;
+                    *reinterpret_cast<float4*>(o + yB) = fB;
+                }
+                // Simpson weights along the row: even columns 2, odd 4,
+                // columns 0 and n - 1 one
+                float e = (fA.x + fA.z) + (fB.x + fB.z);
+                float od = (fA.y + fA.w) + (fB.y + fB.w);
+                if (first) {
+                    e -= 0.5f * fA.x;
+                }
+                if (last) {
+                    od -= 0.75f * fB.w;
+                }
+                return fmaf(4.f, od, 2.f * e);
+            };
+            // the row sums of 4 consecutive output rows X..X+3 (partials
+            // p0..p3 of every lane): reduce-scatter over the segment, the
+            // row's sum stored by one lane
+            auto flush = [&](int X, float p0, float p1, float p2, float p3) {
+                const bool u1 = (l & hs) != 0;
+                float k0 = u1 ? p2 : p0, k1 = u1 ? p3 : p1;
+                const float s0 = u1 ? p0 : p2, s1 = u1 ? p1 : p3;
+                k0 += __shfl_xor_sync(0xffffffffu, s0, hs, seg);
+                k1 += __shfl_xor_sync(0xffffffffu, s1, hs, seg);
+                const bool u2 = (l & qs) != 0;
+                float v = u2 ? k1 : k0;
+                v += __shfl_xor_sync(0xffffffffu, u2 ? k0 : k1, qs, seg);
+                for (int o = qs >> 1; o > 0; o >>= 1) {
+                    v += __shfl_xor_sync(0xffffffffu, v, o, seg);
+                }
+                const int r = (u1 ? 2 : 0) + (u2 ? 1 : 0);
+                if ((l & (qs - 1)) == 0 && X + r < xend) {
+                    pout[B.prof_off + X + r] = h03 * v;
+                }
+            };
+            for (int X = x0 + ra; X < x0 + ra + per; X += 4) {
+                const float p0 = one(X, a0, a1, a2, a3, b0, b1, b2, b3);
+                const float p1 = one(X + 1, a1, a2, a3, a0, b1, b2, b3, b0);
+                const float p2 = one(X + 2, a2, a3, a0, a1, b2, b3, b0, b1);
+                const float p3 = one(X + 3, a3, a0, a1, a2, b3, b0, b1, b2);
+                flush(X, p0, p1, p2, p3);
+            }
+        }
+        mc = mn;
+        lo_c = lo_n;
+        hi_c = hi_n;
+    }
+    if (bad && threadIdx.x == 0) {
+        atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
+    }
+}
+
+}  // namespace

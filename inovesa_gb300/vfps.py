@@ -792,6 +792,16 @@ class BunchBatch(_Handle):
                                           C.byref(rows)))
         return launches.value, rows.value
 
+    KERNELS = ("k_bmaps0f", "k_bmaps0", "k_bmaps0<4>", "k_bmaps0w",
+               "k_bmaps1")
+
+    def kernel_tiles(self):
+        """Tiles each maps kernel of the step walks, by kernel name."""
+        t = (C.c_uint32 * len(self.KERNELS))()
+        self._check(lib().vfps_batch_kernel_tiles(self._h, t,
+                                                  len(self.KERNELS)))
+        return dict(zip(self.KERNELS, list(t)))
+
     def set_wake_mode(self, mode):
         """0: wake potentials on the CUDA cores (default); 1: on the tensor
         cores (TF32 split products, FP32 accumulation)."""

@@ -315,3 +315,51 @@ def test_batch_run_end_to_end(gpu_ctx):
     assert rel_l1(out, after10) <= 1e-6
     assert np.all(np.abs(fill - 1) < 1e-2)
     assert np.all(prof.reshape(3, n).sum(1) > 0)
+
+
+def test_fast_ring_kernel(gpu_ctx, monkeypatch):
+    """The benchmark's lattice (256 rows, 1000 steps per period, centred
+    mesh) runs on the fast ring kernel (composite y-kick, sliding-window
+    drift); the same batch on the classic ring kernel agrees with it to
+    rounding (the two kicks in one stencil; 2e-5 relative L1 after 40
+    steps) and both meet the bar against FP64.  A lattice whose drift
+    shift changes inside a group of 4 energy columns (50 steps per period)
+    stays on the classic kernel."""
+    n = 256
+    p0 = P.derive(GridSize=n, StepsPerTs=1000, padding=2.0)
+    gap = 0.006 * p0["R_bend"]
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(
+        P.derive(GridSize=n, StepsPerTs=1000, padding=2.0, VacuumGap=gap)))
+    specs = []
+    for S in (0.01, 0.2, 0.7, 1.5):
+        p = P.derive(GridSize=n, StepsPerTs=1000, padding=2.0,
+                     VacuumGap=gap, S_csr=S,
+                     RenormalizeCharge=(7 if S == 0.7 else 0))
+        specs.append((p, 0, p["Ib"], 4, False))
+    steps = 40
+    fast = make_batch(gpu_ctx, specs, {n: z})
+    tiles = fast.kernel_tiles()
+    assert tiles["k_bmaps0f"] > 0 and tiles["k_bmaps0"] == 0, tiles
+    fast.step(steps)
+    monkeypatch.setenv("VFPS_RING_KERNEL", "classic")
+    classic = make_batch(gpu_ctx, specs, {n: z})
+    tiles = classic.kernel_tiles()
+    assert tiles["k_bmaps0f"] == 0 and tiles["k_bmaps0"] > 0, tiles
+    classic.step(steps)
+    assert gpu_ctx.device_status() == 0
+    a, b = fast.download(), classic.download()
+    for i, (p, ch, ib, it, cl) in enumerate(specs):
+        off, _ = fast.layout(i)
+        ga = a[off:off + n * n].reshape(n, n)
+        gb = b[off:off + n * n].reshape(n, n)
+        assert rel_l1(ga, gb) <= 2e-5, i
+        ref = oracle_sim(p, ch, ib, z.data(), it=it, clamp=cl)
+        ref.step(steps)
+        assert rel_l1(ga, ref.density(0)) <= TOL, i
+        assert rel_l1(fast.profile(i), ref.profile(0)) <= TOL, i
+    monkeypatch.delenv("VFPS_RING_KERNEL")
+    p = P.derive(GridSize=n, StepsPerTs=50, padding=2.0, VacuumGap=0.0318,
+                 S_csr=0.3)
+    odd = make_batch(gpu_ctx, [(p, 0, p["Ib"], 4, False)], {n: z})
+    tiles = odd.kernel_tiles()
+    assert tiles["k_bmaps0f"] == 0 and tiles["k_bmaps0"] > 0, tiles

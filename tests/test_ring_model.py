@@ -36,7 +36,43 @@ def tiles_of(bunches, tile_cells):
 EMPTY = []   # (bunch, lo, hi) of continuation tiles staging no mesh row
 
 
-def walk(bunches, tiles, rb, c, nctas):
+def window_walk(bunches, b, x0, rows, rb, off, ring, nthreads=128):
+    """Stage 2 of k_bmaps0f (inovesa_gb300/csrc/ring_fast.cuh) on one
+    tile: every segment of n/8 lanes walks its run of output rows in steps
+    of 4 with a window of 4 staged rows per column group, the window's
+    ring offset advanced one slot per row from a start reduced modulo the
+    ring.  For every drift shift the mesh can have, the rows a valid output
+    row reads must be in the slots the walk loads (and every load must stay
+    inside the ring, also for rows past the tile)."""
+    n, hlo, hhi = bunches[b]
+    seg = n // 8
+    rp = nthreads // seg
+    per = -(-rows // rp)
+    steps = -(-per // 4) * 4
+    checked = 0
+    for sh in range(-hlo, hhi - 3 + 1):
+        for rl in range(rp):
+            ra = rl * per
+            xend = x0 + min(rows, ra + per)
+            q = (x0 + ra + sh + off) % rb          # slot0
+            win = []
+            for j in range(3):
+                win.append(q)
+                q = q + 1 if q + 1 < rb else 0
+            for X in range(x0 + ra, x0 + ra + steps):
+                win.append(q)                      # row X + sh + 3
+                q = q + 1 if q + 1 < rb else 0
+                assert all(0 <= w < rb for w in win)
+                if X < xend:
+                    for j in range(4):
+                        assert ring.get(win[j]) == (b, X + sh + j), (
+                            "window row", b, X, sh, j)
+                        checked += 1
+                win.pop(0)
+    return checked
+
+
+def walk(bunches, tiles, rb, c, nctas, windows=False):
     """One CTA's chunk, as the kernel walks it; raises on a violation."""
     ntiles = len(tiles)
     t_begin, t_end = c * ntiles // nctas, (c + 1) * ntiles // nctas
@@ -77,6 +113,8 @@ def walk(bunches, tiles, rb, c, nctas):
             assert ring.get(s) == (b, x), ("row missing", b, x, s)
             reads[s] = x
             checked += 1
+        if windows and n <= 256:
+            checked += window_walk(bunches, b, x0, rows, rb, off, ring)
         if tid + 1 < t_end:
             bn, xn, rn = tiles[tid + 1]
             _, hlo_n, hhi_n = bunches[bn]
@@ -113,6 +151,19 @@ def test_ring_staging_invariants(mix, tile_cells):
     for nctas in sorted({1, 3, 7, max(1, len(tiles) // 3), len(tiles)}):
         for c in range(nctas):
             total += walk(bunches, tiles, rb, c, nctas)
+    assert total > 0
+
+
+@pytest.mark.parametrize("mix", ["scan 256", "narrow halos", "wide halos",
+                                 "short tails"])
+@pytest.mark.parametrize("tile_cells", [2048, 4096, 8192])
+def test_fast_ring_windows(mix, tile_cells):
+    bunches = MIXES[mix]
+    tiles, rb = tiles_of(bunches, tile_cells)
+    total = 0
+    for nctas in sorted({1, 5, max(1, len(tiles) // 2)}):
+        for c in range(nctas):
+            total += walk(bunches, tiles, rb, c, nctas, windows=True)
     assert total > 0
 
 
