@@ -2053,25 +2053,42 @@ k_bmaps0(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
 
 // --------------------------------------------------------------- chain 1
 struct Smem1 {
-    size_t a, b, s, part, total;
+    size_t a, b, s, part, cols, total;
 };
 
-// A = staged rows [nr][n + 4] (2 zero columns each side), B = rotated rows
-// [rows][n + ROWPAD] (pre-shifted by the wake kick), S = RowStencil[rows],
-// part = [rows][8]; t3 reuses A.
+// A = staged rows [nr][n + 8] (4 zero columns each side, 16-byte aligned
+// rows), B = rotated rows [rows][n + ROWPAD] (pre-shifted by the wake
+// kick), S = RowStencil[rows], part = [rows][8], cols = sin(-a) p[y] and
+// cos(-a) p[y] [2][n]; t3 reuses A.
 __host__ __device__ inline Smem1 smem1(int n, int nr, int rows)
 {
     Smem1 L;
     L.a = 0;
-    const size_t a_rows = size_t(nr) * (n + 4);
+    const size_t a_rows = size_t(nr) * (n + 8);
     const size_t t_rows = size_t(rows) * (n + 2 * TPAD);
     L.b = align16(L.a + sizeof(float) * (a_rows > t_rows ? a_rows : t_rows));
     L.s = align16(L.b + sizeof(float) * size_t(rows) * (n + ROWPAD));
     L.part = align16(L.s + sizeof(RowStencil) * rows);
-    L.total = align16(L.part + sizeof(float) * size_t(rows) * 8);
+    L.cols = align16(L.part + sizeof(float) * size_t(rows) * 8);
+    L.total = align16(L.cols + sizeof(float) * 2 * size_t(n));
     return L;
 }
 
+// Chain 1 (the rotation scheme: RotationMap, wake kick, Fokker-Planck) on
+// a tile of rows, one CTA per tile.  Warps own whole rows in every stage:
+//  staging   the tile's rows with the rotation's halo, 16-byte loads, times
+//            the renormalisation factor;
+//  rotation  (src/SM/RotationMap.cpp:97-260) every output cell from the
+//            16 taps of its source cell's neighbourhood; the source
+//            coordinates (cos q - sin p)/dq + zbq and (sin q + cos p)/dp
+//            + zbp from per-row and per-column products and the
+//            reciprocals of dq and dp (the reference divides; the base
+//            cell can differ where a coordinate lies within one rounding
+//            of an integer); truncation toward zero, off-mesh bases give
+//            0, taps off the mesh read the zero halo; with clamping the
+//            result is held within the 2x2 nearest taps as the CPU path
+//            does.  Rows are written pre-shifted by the row's wake kick;
+//  wake kick, Fokker-Planck, new rows and projections.
 __global__ void __launch_bounds__(THREADS, 2)
 k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          const float* __restrict__ tabs, const float* __restrict__ fp5,
@@ -2093,11 +2110,15 @@ k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     float* Bs = reinterpret_cast<float*>(base + L.b);
     RowStencil* S = reinterpret_cast<RowStencil*>(base + L.s);
     float* part = reinterpret_cast<float*>(base + L.part);
+    float* snp = reinterpret_cast<float*>(base + L.cols);
+    float* csp = snp + n;
     const int it = int(B.it);
     const float fac = factor[t.bunch];
-    const int astride = n + 4;
+    const int astride = n + 8;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int NW = THREADS / 32;
 
-    // wake kick of the tile rows
+    // wake kick of the tile rows; the rotation's column products
     for (int r = threadIdx.x; r < rows; r += THREADS) {
         RowStencil sa;
         if (B.flags & F_WAKE) {
@@ -2109,112 +2130,163 @@ k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         }
         S[r] = sa;
     }
-    // stage rows x0-hlo .. x0+rows+hhi with 2 zero columns on each side
+    {
+        const float* pv = tabs + B.tab_off + TAB_P * n;
+        for (int y = threadIdx.x; y < n; y += THREADS) {
+            const float p = pv[y];
+            snp[y] = __fmul_rn(B.sn, p);
+            csp[y] = __fmul_rn(B.cs, p);
+        }
+    }
+    // stage rows x0-hlo .. x0+rows+hhi with 4 zero columns on each side
     {
         const float* src = din + B.dens_off;
-        const int total = nr * astride;
-        for (int i = threadIdx.x; i < total; i += THREADS) {
-            const int r = i / astride, j = i % astride;
-            const int x = x0 - hlo + r, y = j - 2;
-            float v = 0.f;
-            if (unsigned(x) < unsigned(n) && unsigned(y) < unsigned(n)) {
-                v = __ldg(src + size_t(x) * n + y) * fac;
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        const int nq = n >> 2;
+        for (int r = warp; r < nr; r += NW) {
+            const int x = x0 - hlo + r;
+            float4* arow = reinterpret_cast<float4*>(A + size_t(r) * astride);
+            const bool in = unsigned(x) < unsigned(n);
+            const float4* srow = reinterpret_cast<const float4*>(
+                src + size_t(in ? x : 0) * n);
+            for (int c = lane; c < nq; c += 32) {
+                float4 v = z;
+                if (in) {
+                    v = __ldg(srow + c);
+                    v.x *= fac;
+                    v.y *= fac;
+                    v.z *= fac;
+                    v.w *= fac;
+                }
+                arow[1 + c] = v;
             }
-            A[i] = v;
+            if (lane == 0) {
+                arow[0] = z;
+                arow[1 + nq] = z;
+            }
         }
     }
     __syncthreads();
 
-    // rotation (src/SM/RotationMap.cpp:97-260) of the tile rows; each
-    // output is written pre-shifted by its row's wake kick shift
+    // rotation of the tile rows, each output written pre-shifted by its
+    // row's wake kick shift
     {
         const float* qv = tabs + B.tab_off + TAB_Q * n;
-        const float* pv = tabs + B.tab_off + TAB_P * n;
         const int h = int(B.rot_h);
         const bool clamp = B.flags & F_CLAMP;
         const float cell0 = din[B.dens_off] * fac;
         const int bstride = n + ROWPAD;
-        for (int i = threadIdx.x; i < rows * bstride; i += THREADS) {
-            const int r = i / bstride, j = i % bstride;
-            const int y0 = j + S[r].shift0;     // mesh column of this slot
-            float v = 0.f;
-            if (unsigned(y0) < unsigned(n)) {
-                const int xo = x0 + r;
-                const float q = qv[xo], p = pv[y0];
-                const float x1r = fadd(fdiv(fsub(fmul(B.cs, q), fmul(B.sn, p)),
-                                            B.dq), B.zbq);
-                const float y1r = fadd(fdiv(fadd(fmul(B.sn, q), fmul(B.cs, p)),
-                                            B.dp), B.zbp);
-                int x1 = 0, y1 = 0;
-                float xf, yf;
-                const bool okx = base_index(x1r, B.n, &x1, &xf);
-                const bool oky = base_index(y1r, B.n, &y1, &yf);
-                const bool ok = okx && oky;
-                if (ok) {
-                    float icq[4], icp[4];
-                    coefficients(icq, xf, it);
-                    coefficients(icp, yf, it);
-                    // staged row of tap i1: x1 + i1 - h - (x0 - hlo)
-                    const float* srow = A + size_t(x1 - h - x0 + hlo) * astride
-                                        + (y1 - h + 2);
+        const float inv_dq = 1.f / B.dq, inv_dp = 1.f / B.dp;
+        for (int r = warp; r < rows; r += NW) {
+            const int xo = x0 + r;
+            const float q = qv[xo];
+            const float cq = __fmul_rn(B.cs, q), sq = __fmul_rn(B.sn, q);
+            const int sh = S[r].shift0;
+            float* brow = Bs + size_t(r) * bstride;
+            // staged row of tap i1 of base x1: x1 + i1 - h - (x0 - hlo)
+            const int row0 = hlo - h - x0;
+            for (int j = lane; j < bstride; j += 32) {
+                const int y0 = j + sh;            // mesh column of this slot
+                float v = 0.f;
+                if (unsigned(y0) < unsigned(n)) {
+                    const float x1r = __fmaf_rn(__fsub_rn(cq, snp[y0]),
+                                                inv_dq, B.zbq);
+                    const float y1r = __fmaf_rn(__fadd_rn(sq, csp[y0]),
+                                                inv_dp, B.zbp);
+                    int x1 = 0, y1 = 0;
+                    float xf, yf;
+                    const bool okx = base_index(x1r, B.n, &x1, &xf);
+                    const bool oky = base_index(y1r, B.n, &y1, &yf);
+                    const bool ok = okx && oky;
+                    const float* srow = A + size_t(x1 + row0) * astride
+                                        + (y1 - h + 4);
+                    float tap[4][4];
+                    if (ok) {
+                        float icq[4], icp[4];
+                        coefficients(icq, xf, it);
+                        coefficients(icp, yf, it);
 #pragma unroll
-                    for (int i1 = 0; i1 < 4; i1++) {
-                        if (i1 < it) {
-                            const float* rr = srow + size_t(i1) * astride;
-                            float rv = 0.f;
+                        for (int i1 = 0; i1 < 4; i1++) {
+                            if (i1 < it) {
+                                const float* rr = srow + size_t(i1) * astride;
+                                float rv = 0.f;
 #pragma unroll
-                            for (int j1 = 0; j1 < 4; j1++) {
-                                if (j1 < it) {
-                                    rv = fmaf(rr[j1], icp[j1], rv);
+                                for (int j1 = 0; j1 < 4; j1++) {
+                                    if (j1 < it) {
+                                        tap[i1][j1] = rr[j1];
+                                        rv = fmaf(tap[i1][j1], icp[j1], rv);
+                                    }
                                 }
+                                v = fmaf(rv, icq[i1], v);
                             }
-                            v = fmaf(rv, icq[i1], v);
                         }
                     }
-                }
-                if (clamp) {
-                    // 2x2 nearest taps; taps off the mesh read cell (0,0)
-                    float hi = FLT_MIN, lo = FLT_MAX;
+                    if (clamp) {
+                        // 2x2 nearest taps; taps off the mesh read cell
+                        // (0,0), as the CPU path's clamp does
+                        float hi = FLT_MIN, lo = FLT_MAX;
 #pragma unroll
-                    for (int i1 = 1; i1 <= 2; i1++) {
+                        for (int i1 = 1; i1 <= 2; i1++) {
 #pragma unroll
-                        for (int j1 = 1; j1 <= 2; j1++) {
-                            const int i0 = x1 + i1 - h, j0 = y1 + j1 - h;
-                            const bool inm = ok && unsigned(i0) < unsigned(n)
-                                             && unsigned(j0) < unsigned(n);
-                            const float sv = inm
-                                ? A[size_t(i0 - x0 + hlo) * astride + j0 + 2]
-                                : cell0;
-                            hi = (hi < sv) ? sv : hi;
-                            lo = (sv < lo) ? sv : lo;
+                            for (int j1 = 1; j1 <= 2; j1++) {
+                                const int i0 = x1 + i1 - h, j0 = y1 + j1 - h;
+                                const bool inm = ok
+                                    && unsigned(i0) < unsigned(n)
+                                    && unsigned(j0) < unsigned(n);
+                                const float sv = inm ? tap[i1][j1] : cell0;
+                                hi = (hi < sv) ? sv : hi;
+                                lo = (sv < lo) ? sv : lo;
+                            }
                         }
+                        const float tmin = (v < hi) ? v : hi;
+                        v = (tmin < lo) ? lo : tmin;
                     }
-                    const float tmin = (v < hi) ? v : hi;
-                    v = (tmin < lo) ? lo : tmin;
                 }
+                brow[j] = v;
             }
-            Bs[i] = v;
         }
     }
     __syncthreads();
 
     // wake y-kick: t3[x][y] = sum_j w_j t2[x][y + shift0 + j], the row of
-    // Bs already starts at shift0; t3 goes to A with TPAD zero columns
+    // Bs already starts at shift0; t3 goes to A with TPAD zero columns.
+    // Lane segments of n/8 lanes own 8 columns of a row each.
     float* T = A;
     const int tstride = n + 2 * TPAD;
-    for (int i = threadIdx.x; i < rows * tstride; i += THREADS) {
-        const int r = i / tstride, j = i % tstride;
-        const int y = j - TPAD;
-        float v = 0.f;
-        if (unsigned(y) < unsigned(n)) {
+    {
+        const int seg = n >> 3;
+        const int lg = lg_seg(n);
+        const int rp = THREADS >> lg;
+        const int l = threadIdx.x & (seg - 1);
+        const int y = 8 * l;
+        for (int r = threadIdx.x >> lg; r < rows; r += rp) {
             const RowStencil s = S[r];
-            const float* br = Bs + size_t(r) * (n + ROWPAD) + y;
-            v = s.w[0] * br[0];
-            v = fmaf(s.w[1], br[1], v);
-            v = fmaf(s.w[2], br[2], v);
-            v = fmaf(s.w[3], br[3], v);
+            const float4* br = reinterpret_cast<const float4*>(
+                Bs + size_t(r) * (n + ROWPAD) + y);
+            const float4 v0 = br[0], v1 = br[1], v2 = br[2];
+            const float c[12] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y,
+                                 v1.z, v1.w, v2.x, v2.y, v2.z, v2.w};
+            float o[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                float a = s.w[0] * c[k];
+                a = fmaf(s.w[1], c[k + 1], a);
+                a = fmaf(s.w[2], c[k + 2], a);
+                a = fmaf(s.w[3], c[k + 3], a);
+                o[k] = a;
+            }
+            float* trow = T + size_t(r) * tstride;
+            reinterpret_cast<float4*>(trow + TPAD + y)[0] =
+                make_float4(o[0], o[1], o[2], o[3]);
+            reinterpret_cast<float4*>(trow + TPAD + y)[1] =
+                make_float4(o[4], o[5], o[6], o[7]);
+            if (l == 0) {
+                reinterpret_cast<float4*>(trow)[0] =
+                    make_float4(0.f, 0.f, 0.f, 0.f);
+                reinterpret_cast<float4*>(trow + TPAD + n)[0] =
+                    make_float4(0.f, 0.f, 0.f, 0.f);
+            }
         }
-        T[i] = v;
     }
     __syncthreads();
     FpCols fpc;

@@ -121,3 +121,39 @@ def test_uneven_batch_bench_seed(gpu_ctx):
         assert rel_l1(b.profile(i), ref.profile(0)) <= TOL, (i, n, it)
     print("uneven batch: worst density L1 vs FP64 after %d steps %.3g"
           % (steps, worst))
+
+
+def test_batch_sums_against_fp64(gpu_ctx):
+    """The batched step sums in FP32 where the plain path uses FP64: the
+    bunch profile (Simpson row sums of the new density, FP32 partial sums
+    reduced across the row's lanes) and the charge (a compensated FP32 sum
+    of the profile, about 48 significant bits).  Bounds against FP64 sums
+    of the same data, on the benchmark's scan after 30 steps: profile
+    relative L1 <= 1e-6 and largest row error <= 1e-5 of the peak; charge
+    within 1e-12 of the FP64 sum of the same profile, and within 1e-6 of
+    the FP64 double sum over the density."""
+    p, gap, currents = bench.workload_params()
+    n = p["ps_bins"]
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    batch = bench.make_batch(gpu_ctx, p, currents, z)
+    batch.step(29)
+    dens = batch.download().reshape(256, n, n).astype(np.float64)
+    profs = [np.asarray(batch.profile(i), np.float64) for i in range(256)]
+    # the filling after a step is the charge of the state it started from
+    batch.step(1)
+    fill = batch.filling()
+    ws = np.asarray(oracle.simpson(n, p["axes"][0], p["axes"][1],
+                                   np.float32), np.float64)
+    worst_l1 = worst_max = worst_q = worst_qd = 0.0
+    for i in range(0, 256, 17):
+        prof = profs[i]
+        ref = dens[i] @ ws
+        worst_l1 = max(worst_l1, np.abs(prof - ref).sum() / np.abs(ref).sum())
+        worst_max = max(worst_max, np.abs(prof - ref).max() / ref.max())
+        q64 = float(prof @ ws)
+        worst_q = max(worst_q, abs(fill[i] - q64) / q64)
+        worst_qd = max(worst_qd, abs(fill[i] - float(ref @ ws)) / q64)
+    print("profile L1 %.3g, max %.3g; charge vs FP64 of the profile %.3g, "
+          "of the density %.3g" % (worst_l1, worst_max, worst_q, worst_qd))
+    assert worst_l1 <= 1e-6 and worst_max <= 1e-5
+    assert worst_q <= 1e-12 and worst_qd <= 1e-6
