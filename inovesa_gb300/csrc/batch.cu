@@ -44,7 +44,7 @@ using vfps::DevBuf;
 // ================================================================== host
 enum {
     TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_RINGF = 4,
-    TL_COUNT = 5
+    TL_RINGF128 = 5, TL_RINGF64 = 6, TL_COUNT = 7
 };
 constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel, G = 2
 constexpr int RING4_N = 512;      // the mesh of the ring kernel, G = 4
@@ -56,7 +56,8 @@ struct vfps_batch {
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    // tile lists: TL_RINGF (chain 0, n <= 256, regular lattices: the fast
+    // tile lists: TL_RINGF, TL_RINGF128, TL_RINGF64 (chain 0, n = 256,
+    // 128, 64, regular lattices: the fast
     // ring kernel), TL_RING (the other chain-0 meshes up to 256 rows),
     // TL_RING4 (chain 0, n = 512), TL_ROT (chain 1), TL_WIDE (chain 0,
     // n = 1024)
@@ -87,8 +88,8 @@ struct vfps_batch {
     unsigned gridR = 0;        // persistent CTAs of k_bmaps0
     SmemR layoutR4{};          // the same for the 512-row ring kernel
     unsigned gridR4 = 0;
-    SmemR layoutRF{};          // the same for the fast ring kernel
-    unsigned gridRF = 0;
+    SmemR layoutRF[3] = {};    // the same for the fast ring kernel, per
+    unsigned gridRF[3] = {};   // mesh size 256, 128, 64
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
@@ -233,7 +234,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     // that each fills the SMs the others leave free (no kernel's tail
     // idles the GPU); sequential when the kernels are timed one by one
     int classes = 0;
-    for (int c : {TL_RINGF, TL_RING, TL_RING4, TL_WIDE, TL_ROT}) {
+    for (int c : {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RING, TL_RING4,
+                  TL_WIDE, TL_ROT}) {
         classes += b->htiles[c].empty() ? 0 : 1;
     }
     const bool forked = !ev && classes > 1;
@@ -269,8 +271,12 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             b->dens[to].p, b->prof[to].p, b->ctx->d_status, layout));
         VFPS_LAUNCHED();
     };
-    ring_launch(k_bmaps0f<RTHREADS>, TL_RINGF, b->gridRF, RTHREADS,
-                b->layoutRF, (const RowInfo7*)b->rinfo7.p);
+    ring_launch(k_bmaps0f<RTHREADS, 256>, TL_RINGF, b->gridRF[0], RTHREADS,
+                b->layoutRF[0], (const RowInfo7*)b->rinfo7.p);
+    ring_launch(k_bmaps0f<RTHREADS, 128>, TL_RINGF128, b->gridRF[1],
+                RTHREADS, b->layoutRF[1], (const RowInfo7*)b->rinfo7.p);
+    ring_launch(k_bmaps0f<RTHREADS, 64>, TL_RINGF64, b->gridRF[2], RTHREADS,
+                b->layoutRF[2], (const RowInfo7*)b->rinfo7.p);
     ring_launch(k_bmaps0<2, RTHREADS>, TL_RING, b->gridR, RTHREADS,
                 b->layoutR, (const RowInfo*)b->rinfo.p);
     ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
@@ -328,17 +334,21 @@ void build_tiles(vfps_batch* b, int tile_cells)
     int max_rows = 0;
     // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
-    int ring_rows = 0, ring_n = 0, ring4_rows = 0, ringf_rows = 0,
-        ringf_n = 0;
+    int ring_rows = 0, ring_n = 0, ring4_rows = 0, ringf_rows[3] = {0, 0, 0};
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
         const int c = B.chain == 1 ? TL_ROT
                       : (n <= RING_MAX_N
-                             ? ((B.flags & F_Y7) ? TL_RINGF : TL_RING)
+                             ? ((B.flags & F_Y7)
+                                    ? (n == 256 ? TL_RINGF
+                                                : (n == 128 ? TL_RINGF128
+                                                            : TL_RINGF64))
+                                    : TL_RING)
                              : (n == RING4_N ? TL_RING4 : TL_WIDE));
         int tx = std::max(4, tile_cells / n);
-        if (c == TL_RING || c == TL_RING4 || c == TL_RINGF) {
+        if (c == TL_RING || c == TL_RING4 || c == TL_RINGF
+            || c == TL_RINGF128 || c == TL_RINGF64) {
             // the ring holds two tiles with their halos: at most 32 staged
             // rows per tile keeps it at 64 slots or fewer
             tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
@@ -353,9 +363,9 @@ void build_tiles(vfps_batch* b, int tile_cells)
         if (c == TL_RING) {
             ring_rows = std::max(ring_rows, nr);
             ring_n = std::max(ring_n, n);
-        } else if (c == TL_RINGF) {
-            ringf_rows = std::max(ringf_rows, nr);
-            ringf_n = std::max(ringf_n, n);
+        } else if (c == TL_RINGF || c == TL_RINGF128 || c == TL_RINGF64) {
+            const int k = c == TL_RINGF ? 0 : (c == TL_RINGF128 ? 1 : 2);
+            ringf_rows[k] = std::max(ringf_rows[k], nr);
         } else if (c == TL_RING4) {
             ring4_rows = std::max(ring4_rows, nr);
         } else if (c == TL_WIDE) {
@@ -387,12 +397,23 @@ void build_tiles(vfps_batch* b, int tile_cells)
         L.total = static_cast<uint32_t>(o);
         return o;
     };
-    if (!b->htiles[TL_RINGF].empty()) {
-        b->smem[TL_RINGF] = ring_layout(b->layoutRF, ringf_rows, ringf_n,
-                                        sizeof(RowInfo7));
-        b->gridRF = persistent_grid(b, k_bmaps0f<RTHREADS>, RTHREADS,
-                                    b->smem[TL_RINGF],
-                                    b->htiles[TL_RINGF].size());
+    const int flist[3] = {TL_RINGF, TL_RINGF128, TL_RINGF64};
+    const int fn[3] = {256, 128, 64};
+    for (int k = 0; k < 3; k++) {
+        const int c = flist[k];
+        if (b->htiles[c].empty()) {
+            continue;
+        }
+        b->smem[c] = ring_layout(b->layoutRF[k], ringf_rows[k], fn[k],
+                                 sizeof(RowInfo7));
+        const size_t nt = b->htiles[c].size();
+        b->gridRF[k] =
+            k == 0 ? persistent_grid(b, k_bmaps0f<RTHREADS, 256>, RTHREADS,
+                                     b->smem[c], nt)
+            : k == 1 ? persistent_grid(b, k_bmaps0f<RTHREADS, 128>, RTHREADS,
+                                       b->smem[c], nt)
+                     : persistent_grid(b, k_bmaps0f<RTHREADS, 64>, RTHREADS,
+                                       b->smem[c], nt);
     }
     if (!b->htiles[TL_RING].empty()) {
         b->smem[TL_RING] = ring_layout(b->layoutR, ring_rows, ring_n,
@@ -443,10 +464,18 @@ void upload_tiles(vfps_batch* b)
 {
     VFPS_REQUIRE(tiles_fit(b),
                  "tile of the largest mesh does not fit in shared memory");
-    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADS>,
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADS, 256>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
                                        b->smem[TL_RINGF], 1))));
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADS, 128>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_RINGF128], 1))));
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADS, 64>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_RINGF64], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<2, RTHREADS>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
@@ -1505,6 +1534,10 @@ extern "C" int vfps_batch_kernel_tiles(const vfps_batch* b, uint32_t* tiles,
     const int order[] = {TL_RINGF, TL_RING, TL_RING4, TL_WIDE, TL_ROT};
     for (uint32_t k = 0; k < count && k < 5; k++) {
         tiles[k] = static_cast<uint32_t>(b->htiles[order[k]].size());
+    }
+    if (count > 0) {   // the fast ring kernel: every mesh size
+        tiles[0] += static_cast<uint32_t>(b->htiles[TL_RINGF128].size()
+                                          + b->htiles[TL_RINGF64].size());
     }
     return VFPS_OK;
 }

@@ -120,7 +120,9 @@ __device__ __forceinline__ float4 fp4(const float (&w)[7], const float4& f0,
     return make_float4(o[0], o[1], o[2], o[3]);
 }
 
-template <int NT>
+// N: the mesh size of every bunch of the tile list (64, 128 or 256; the
+// lane mapping, strides and shuffle widths are constants)
+template <int NT, int N>
 __global__ void __launch_bounds__(NT, 3)
 k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
           uint32_t ntiles, const float* __restrict__ tabs,
@@ -134,7 +136,8 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     RowInfo7* S = reinterpret_cast<RowInfo7*>(base + L.s);
     float* T = reinterpret_cast<float*>(base + L.tab);
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
-    const int rb = int(L.rb), rs = int(L.rs);
+    const int rb = int(L.rb);
+    constexpr int rs = N + 2 * APAD + 16;   // astride0(N), the ring's L.rs
     const int ring_floats = rb * rs;
     const int lane = threadIdx.x & 31;
 
@@ -202,14 +205,14 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
         const Tile t = tiles[tid];
         const BDev B = bd[t.bunch];
-        const int n = int(B.n);
+        constexpr int n = N;
         const int x0 = int(t.x0);
         const int rows = int(t.rows);
-        const int seg = n >> 3;              // lanes per row
+        constexpr int seg = N >> 3;          // lanes per row
         const int l = threadIdx.x & (seg - 1);
         const int rl = threadIdx.x / seg;    // segment
-        const int rp = NT / seg;             // segments
-        const int as = astride0(n);
+        constexpr int rp = NT / seg;         // segments
+        constexpr int as = N + 2 * APAD + 16;
         const int yA = 4 * l, yB = (n >> 1) + 4 * l;
 
         // stage 1: both y-kicks of the new rows, in place
@@ -225,13 +228,8 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             for (int i = rl; i < m; i += rp) {
                 const int x = lo_c + i;
                 float* row = ring + size_t(mc.slot(x, rb)) * rs;
-                // zeros right of the row: the slot may have held a longer
-                // row of another bunch
-                if (n + 2 * APAD + 16 < rs) {
-                    for (int j = l; j < (APAD + 16) / 4; j += seg) {
-                        reinterpret_cast<float4*>(row + APAD + n)[j] = z;
-                    }
-                }
+                // (every row of the list has n columns: the zeros right of
+                // a staged row, written when the ring was cleared, stay)
                 if (unsigned(x) < unsigned(n)) {
                     const float4 q0 = reinterpret_cast<const float4*>(S + i)[0];
                     const float4 q1 = reinterpret_cast<const float4*>(S + i)[1];
