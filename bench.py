@@ -14,7 +14,8 @@ Prints one JSON line (rank 0).  Besides the headline it carries, under
 "configs", the other workloads of the benchmark plan measured in the same
 run: the plain single bunch on the rotation chain (256x256, 500 steps per
 period), the bursting 512x512 bunch with CSR power every step, the uneven
-96-bunch batch and the headline scan on the rotation chain.  --impl
+96-bunch batch, the headline scan on the rotation chain and the learned
+warm start (periods to equilibrium against the Gaussian start).  --impl
 reference times the CPU restatement of the reference solver loop (the
 oracle, float) on all host cores on the same workload.
 """
@@ -477,6 +478,23 @@ def config_uneven(ctx, stream, hbm, cores):
     return out
 
 
+def config_warm_start(ctx):
+    """Learned warm start on 256x256 bunches: the network trained on 512
+    solver equilibria (S ~ U(0.02, 0.45), g/R in 0.004..0.008, damping 5..150
+    synchrotron periods), then periods to equilibrium (profile change below
+    1e-5 per period for three periods, the solver judging) of 24 held-out
+    bunches from the Gaussian start, from the potential-well state alone
+    and from the proposal; and of 24 more at a damping time of 100 periods
+    (the plain single-bunch workload's)."""
+    from inovesa_gb300 import warmstart as W
+    t = time.perf_counter()
+    res, _ = W.experiment(ctx, n=256, spt=1000, ntrain=512, ntest=24,
+                          iters=2000, max_periods=600, seed=11,
+                          report_damping=(100.0,))
+    res["seconds"] = time.perf_counter() - t
+    return res
+
+
 def config_scan_rotation(ctx, stream, hbm, p, currents, z):
     """The current scan of the headline on the rotation chain (cubic
     RotationMap, wake kick, Fokker-Planck; the batched k_bmaps1): rate,
@@ -735,7 +753,8 @@ def main():
                 ("uneven_96", lambda: config_uneven(ctx, stream, hbm, cores)),
                 ("scan_rotation_chain",
                  lambda: config_scan_rotation(ctx, stream, hbm, p, currents,
-                                              z))):
+                                              z)),
+                ("warm_start_256", lambda: config_warm_start(ctx))):
             try:
                 cfgs[key] = fn()
             except Exception as e:   # reported, the headline stands

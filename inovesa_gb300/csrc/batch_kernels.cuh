@@ -2074,6 +2074,96 @@ __host__ __device__ inline Smem1 smem1(int n, int nr, int rows)
     return L;
 }
 
+// The rotation (src/SM/RotationMap.cpp:97-260) of a tile's rows from the
+// staged rows A ([nr][n + 8], 4 zero columns each side) into Bs
+// ([rows][n + ROWPAD], slot j of row r holds mesh column j + the row's
+// wake kick shift), for interpolation with IT points per axis (the
+// reference's calcCoefficiants, src/SM/SourceMap.cpp:142-170) and, when
+// CLAMP, the CPU path's clamp to the 2x2 nearest taps.  A warp per row,
+// lanes across the slots.
+template <int IT, bool CLAMP>
+__device__ __forceinline__ void rotate_rows(
+    const BDev& B, int x0, int rows, int hlo, const float* __restrict__ tabs,
+    const float* __restrict__ din, float fac, const float* A, float* Bs,
+    const RowStencil* S, const float* snp, const float* csp)
+{
+    const int n = int(B.n);
+    const int astride = n + 8;
+    const int bstride = n + ROWPAD;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int NW = THREADS / 32;
+    constexpr int h = (IT - 1) / 2;
+    const float* qv = tabs + B.tab_off + TAB_Q * n;
+    const float cell0 = CLAMP ? din[B.dens_off] * fac : 0.f;
+    const float inv_dq = 1.f / B.dq, inv_dp = 1.f / B.dp;
+    const float zbq = B.zbq, zbp = B.zbp;
+    // staged row of tap i1 of base x1: x1 + i1 - h - (x0 - hlo)
+    const int row0 = hlo - h - x0;
+    for (int r = warp; r < rows; r += NW) {
+        const float q = qv[x0 + r];
+        const float cq = __fmul_rn(B.cs, q), sq = __fmul_rn(B.sn, q);
+        const int sh = S[r].shift0;
+        float* brow = Bs + size_t(r) * bstride;
+        for (int j = lane; j < bstride; j += 32) {
+            const int y0 = j + sh;            // mesh column of this slot
+            float v = 0.f;
+            if (unsigned(y0) < unsigned(n)) {
+                const float x1r = __fmaf_rn(__fsub_rn(cq, snp[y0]), inv_dq,
+                                            zbq);
+                const float y1r = __fmaf_rn(__fadd_rn(sq, csp[y0]), inv_dp,
+                                            zbp);
+                int x1 = 0, y1 = 0;
+                float xf, yf;
+                const bool okx = base_index(x1r, B.n, &x1, &xf);
+                const bool oky = base_index(y1r, B.n, &y1, &yf);
+                const bool ok = okx && oky;
+                float tap[IT][IT];
+                if (ok) {
+                    float icq[4], icp[4];
+                    coefficients(icq, xf, IT);
+                    coefficients(icp, yf, IT);
+                    const float* srow = A + size_t(x1 + row0) * astride
+                                        + (y1 - h + 4);
+#pragma unroll
+                    for (int i1 = 0; i1 < IT; i1++) {
+                        const float* rr = srow + i1 * astride;
+                        float rv = 0.f;
+#pragma unroll
+                        for (int j1 = 0; j1 < IT; j1++) {
+                            tap[i1][j1] = rr[j1];
+                            rv = fmaf(tap[i1][j1], icp[j1], rv);
+                        }
+                        v = fmaf(rv, icq[i1], v);
+                    }
+                }
+                if (CLAMP) {
+                    // 2x2 nearest taps; taps off the mesh read cell (0,0),
+                    // as the CPU path's clamp does
+                    float hi = FLT_MIN, lo = FLT_MAX;
+#pragma unroll
+                    for (int i1 = 1; i1 <= 2; i1++) {
+#pragma unroll
+                        for (int j1 = 1; j1 <= 2; j1++) {
+                            const int i0 = x1 + i1 - h, j0 = y1 + j1 - h;
+                            const bool inm = ok
+                                && unsigned(i0) < unsigned(n)
+                                && unsigned(j0) < unsigned(n);
+                            const float sv = inm ? tap[i1 < IT ? i1 : 0]
+                                                      [j1 < IT ? j1 : 0]
+                                                 : cell0;
+                            hi = (hi < sv) ? sv : hi;
+                            lo = (sv < lo) ? sv : lo;
+                        }
+                    }
+                    const float tmin = (v < hi) ? v : hi;
+                    v = (tmin < lo) ? lo : tmin;
+                }
+            }
+            brow[j] = v;
+        }
+    }
+}
+
 // Chain 1 (the rotation scheme: RotationMap, wake kick, Fokker-Planck) on
 // a tile of rows, one CTA per tile.  Warps own whole rows in every stage:
 //  staging   the tile's rows with the rotation's halo, 16-byte loads, times
@@ -2089,7 +2179,7 @@ __host__ __device__ inline Smem1 smem1(int n, int nr, int rows)
 //            result is held within the 2x2 nearest taps as the CPU path
 //            does.  Rows are written pre-shifted by the row's wake kick;
 //  wake kick, Fokker-Planck, new rows and projections.
-__global__ void __launch_bounds__(THREADS, 2)
+__global__ void __launch_bounds__(THREADS, 3)
 k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
          const float* __restrict__ tabs, const float* __restrict__ fp5,
          const float* __restrict__ wake, const float* __restrict__ factor,
@@ -2169,81 +2259,28 @@ k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     __syncthreads();
 
     // rotation of the tile rows, each output written pre-shifted by its
-    // row's wake kick shift
+    // row's wake kick shift (the interpolation order and the clamp are
+    // the bunch's: one instance each, chosen once per tile)
     {
-        const float* qv = tabs + B.tab_off + TAB_Q * n;
-        const int h = int(B.rot_h);
         const bool clamp = B.flags & F_CLAMP;
-        const float cell0 = din[B.dens_off] * fac;
-        const int bstride = n + ROWPAD;
-        const float inv_dq = 1.f / B.dq, inv_dp = 1.f / B.dp;
-        for (int r = warp; r < rows; r += NW) {
-            const int xo = x0 + r;
-            const float q = qv[xo];
-            const float cq = __fmul_rn(B.cs, q), sq = __fmul_rn(B.sn, q);
-            const int sh = S[r].shift0;
-            float* brow = Bs + size_t(r) * bstride;
-            // staged row of tap i1 of base x1: x1 + i1 - h - (x0 - hlo)
-            const int row0 = hlo - h - x0;
-            for (int j = lane; j < bstride; j += 32) {
-                const int y0 = j + sh;            // mesh column of this slot
-                float v = 0.f;
-                if (unsigned(y0) < unsigned(n)) {
-                    const float x1r = __fmaf_rn(__fsub_rn(cq, snp[y0]),
-                                                inv_dq, B.zbq);
-                    const float y1r = __fmaf_rn(__fadd_rn(sq, csp[y0]),
-                                                inv_dp, B.zbp);
-                    int x1 = 0, y1 = 0;
-                    float xf, yf;
-                    const bool okx = base_index(x1r, B.n, &x1, &xf);
-                    const bool oky = base_index(y1r, B.n, &y1, &yf);
-                    const bool ok = okx && oky;
-                    const float* srow = A + size_t(x1 + row0) * astride
-                                        + (y1 - h + 4);
-                    float tap[4][4];
-                    if (ok) {
-                        float icq[4], icp[4];
-                        coefficients(icq, xf, it);
-                        coefficients(icp, yf, it);
-#pragma unroll
-                        for (int i1 = 0; i1 < 4; i1++) {
-                            if (i1 < it) {
-                                const float* rr = srow + size_t(i1) * astride;
-                                float rv = 0.f;
-#pragma unroll
-                                for (int j1 = 0; j1 < 4; j1++) {
-                                    if (j1 < it) {
-                                        tap[i1][j1] = rr[j1];
-                                        rv = fmaf(tap[i1][j1], icp[j1], rv);
-                                    }
-                                }
-                                v = fmaf(rv, icq[i1], v);
-                            }
-                        }
-                    }
-                    if (clamp) {
-                        // 2x2 nearest taps; taps off the mesh read cell
-                        // (0,0), as the CPU path's clamp does
-                        float hi = FLT_MIN, lo = FLT_MAX;
-#pragma unroll
-                        for (int i1 = 1; i1 <= 2; i1++) {
-#pragma unroll
-                            for (int j1 = 1; j1 <= 2; j1++) {
-                                const int i0 = x1 + i1 - h, j0 = y1 + j1 - h;
-                                const bool inm = ok
-                                    && unsigned(i0) < unsigned(n)
-                                    && unsigned(j0) < unsigned(n);
-                                const float sv = inm ? tap[i1][j1] : cell0;
-                                hi = (hi < sv) ? sv : hi;
-                                lo = (sv < lo) ? sv : lo;
-                            }
-                        }
-                        const float tmin = (v < hi) ? v : hi;
-                        v = (tmin < lo) ? lo : tmin;
-                    }
-                }
-                brow[j] = v;
+        switch (it) {
+        case 2:
+            rotate_rows<2, false>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
+                                  S, snp, csp);
+            break;
+        case 3:
+            rotate_rows<3, false>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
+                                  S, snp, csp);
+            break;
+        default:
+            if (clamp) {
+                rotate_rows<4, true>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
+                                     S, snp, csp);
+            } else {
+                rotate_rows<4, false>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
+                                      S, snp, csp);
             }
+            break;
         }
     }
     __syncthreads();

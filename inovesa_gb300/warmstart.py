@@ -28,13 +28,21 @@ from . import vfps as V
 
 NIN, NH, NLAT = 3, 128, 32
 GAP_LO, GAP_HI = 0.004, 0.008
+# damping times of the training domain, in synchrotron periods: from
+# strongly damped rings to the reference's default lattice (about 135
+# periods at 1000 steps per period) and the 100 periods of the plain
+# single-bunch workload
+TD_LO, TD_HI = 5.0, 150.0
 
 
 def normalise_inputs(S, gap_ratio, damping_periods):
-    """Network inputs, each about unit range over the training domain."""
+    """Network inputs, each about unit range over the training domain (the
+    damping time on a log scale)."""
+    lo, hi = math.log(TD_LO), math.log(TD_HI)
+    td = np.log(np.asarray(damping_periods, np.float64))
     return np.stack([np.asarray(S, np.float64) / 0.25 - 1.0,
                      (np.asarray(gap_ratio, np.float64) - 0.006) / 0.002,
-                     (np.asarray(damping_periods, np.float64) - 10.0) / 5.0],
+                     (2.0 * td - (lo + hi)) / (hi - lo)],
                     axis=-1).astype(np.float32)
 
 
@@ -46,15 +54,24 @@ def bunch_params(n, spt, S, gap_ratio, damping_periods):
                     S_csr=float(S), DampingTime=damping_periods / base["fs"])
 
 
+# a bunch counts as at equilibrium once the profile change has stayed below
+# the tolerance for this many periods in a row (the profile is sampled
+# once per synchrotron period, and a coherent oscillation can make a
+# single sample look still)
+CONFIRM = 3
+
+
 def run_to_equilibrium(ctx, samples, n=256, spt=1000, tol=1e-5,
-                       max_periods=400, start=None):
+                       max_periods=400, start=None, confirm=CONFIRM):
     """Advance one batch of bunches period by period until the relative L1
-    change of each profile over a period is below tol.
+    change of each profile over a period has been below tol for `confirm`
+    periods in a row.
 
     samples: (S, gap ratio, damping periods) per bunch; start: initial
     densities [nb][n][n], "potential_well" (the device's potential-well
     state) or None (the Gaussian).  Returns (final densities [nb][n][n],
-    periods needed per bunch (-1: not converged))."""
+    periods to equilibrium per bunch: the first period of the run of
+    `confirm` quiet periods (-1: not converged))."""
     zs, keys, descs = {}, [], []
     for S, g, td in samples:
         p = bunch_params(n, spt, S, g, td)
@@ -84,13 +101,15 @@ def run_to_equilibrium(ctx, samples, n=256, spt=1000, tol=1e-5,
         return np.stack([pr[lay[i][1]:lay[i][1] + n] for i in range(nb)])
 
     prev = profiles()
+    streak = np.zeros(nb, int)
     for period in range(1, max_periods + 1):
         b.step(spt)
         cur = profiles()
         change = (np.abs(cur - prev).sum(1)
                   / np.maximum(np.abs(cur).sum(1), 1e-30))
-        newly = (done < 0) & (change < tol)
-        done[newly] = period
+        streak = np.where(change < tol, streak + 1, 0)
+        newly = (done < 0) & (streak >= confirm)
+        done[newly] = period - confirm + 1
         prev = cur
         if np.all(done >= 0):
             break
@@ -291,14 +310,19 @@ def train(net, x, targets, iters=2000, batch=64, lr=1e-3, seed=1):
     return hist
 
 
-def sample_inputs(rng, count, quantise_gap):
-    """(S, gap ratio, damping periods) drawn uniformly from the training
-    domain; training gaps sit on a grid of 9 values (one impedance each)."""
+def sample_inputs(rng, count, quantise_gap, damping=None):
+    """(S, gap ratio, damping periods) drawn from the training domain (S
+    and g/R uniform, the damping time log-uniform, or fixed to `damping`);
+    training gaps sit on a grid of 9 values (one impedance each)."""
     S = rng.uniform(0.02, 0.45, size=count)
     g = rng.uniform(GAP_LO, GAP_HI, size=count)
     if quantise_gap:
         g = np.round(g / 0.0005) * 0.0005
-    td = rng.uniform(5.0, 15.0, size=count)
+    if damping is None:
+        td = np.exp(rng.uniform(math.log(TD_LO), math.log(TD_HI),
+                                size=count))
+    else:
+        td = np.full(count, float(damping))
     return list(zip(S.tolist(), g.tolist(), td.tolist()))
 
 
@@ -316,37 +340,12 @@ def equilibria(ctx, samples, n, spt, tol, max_periods, start=None,
     return np.concatenate(dens), np.concatenate(done)
 
 
-def experiment(ctx, n=256, spt=1000, ntrain=2048, ntest=128, iters=3000,
-               tol=1e-5, max_periods=300, seed=7, log=None, tol_train=None,
-               max_periods_train=None):
-    """Train the correction on solver equilibria, then compare the periods
-    to equilibrium on held-out inputs from the Gaussian, from the
-    potential-well state alone and from the proposal (potential-well state
-    plus the learned correction).  The training equilibria may be
-    converged further than the judging tolerance (tol_train): the stopping
-    rule samples the profile once per synchrotron period and leaves
-    coherent oscillations of about a damping time's worth of the
-    tolerance, which would otherwise be learned as noise."""
-    rng = np.random.default_rng(seed)
-    train_in = sample_inputs(rng, ntrain, True)
-    test_in = sample_inputs(rng, ntest, False)
-    axes = bunch_params(n, spt, *train_in[0])["axes"]
-    dq = (axes[1] - axes[0]) / (n - 1)
-    # training targets: equilibrium (unit charge) minus potential well
-    tr_d, tr_p = equilibria(ctx, train_in, n, spt, tol_train or tol,
-                            max_periods_train or max_periods,
-                            start="potential_well")
-    tr_base = potential_well_states(ctx, train_in, n, spt)
-    ok = tr_p >= 0
-    resid = (simpson_normalise(tr_d[ok], dq).astype(np.float64)
-             - tr_base[ok]).reshape(int(ok.sum()), -1)
-    scale = float(resid.std()) or 1.0
-    x = normalise_inputs(*np.array(train_in)[ok].T)
-    tgt = (resid / scale).astype(np.float32)
-    net = WarmStartNet(ctx, n * n, seed=seed)
-    net.set_bias(tgt.mean(0))
-    hist = train(net, x, tgt, iters=iters)
-    # held out: Gaussian start, potential well, proposal
+def evaluate(ctx, net, test_in, scale, n, spt, tol, max_periods, dq):
+    """Periods to equilibrium of held-out inputs from the Gaussian start,
+    from the potential-well state alone and from the proposal (state plus
+    the learned correction), judged by the solver; the end states of the
+    warm and the Gaussian runs compared."""
+    ntest = len(test_in)
     g_d, g_p = equilibria(ctx, test_in, n, spt, tol, max_periods)
     base = potential_well_states(ctx, test_in, n, spt)
     _, h_p = equilibria(ctx, test_in, n, spt, tol, max_periods,
@@ -366,16 +365,11 @@ def experiment(ctx, n=256, spt=1000, ntrain=2048, ntest=128, iters=3000,
     def med(v):
         return float(np.median(v)) if both.any() else None
 
-    out = {
-        "grid": n, "steps_per_period": spt, "tolerance_per_period": tol,
-        "train_tolerance_per_period": tol_train or tol, "iters": iters,
-        "train_samples": int(ntrain), "train_converged": int(ok.sum()),
-        "residual_scale": scale,
+    return {
         "test_samples": int(ntest), "test_converged_all": int(both.sum()),
         "test_converged_gaussian": int((g_p > 0).sum()),
         "test_converged_potential_well": int((h_p > 0).sum()),
         "test_converged_warm": int((w_p > 0).sum()),
-        "train_loss_first": hist[0], "train_loss_last": hist[-1],
         "periods_gaussian_median": med(g_p[both]),
         "periods_potential_well_median": med(h_p[both]),
         "periods_warm_median": med(w_p[both]),
@@ -384,11 +378,73 @@ def experiment(ctx, n=256, spt=1000, ntrain=2048, ntest=128, iters=3000,
         "speedup_median": med(g_p[both] / np.maximum(w_p[both], 1)),
         "speedup_total": float(g_p[both].sum() / max(w_p[both].sum(), 1))
         if both.any() else None,
+        "warm_faster_than_potential_well": int(
+            (w_p[both] < h_p[both]).sum()),
+        "warm_slower_than_potential_well": int(
+            (w_p[both] > h_p[both]).sum()),
         "potential_well_l1_median": float(np.median(err(base))),
         "proposal_l1_median": float(np.median(err(prop))),
         "same_equilibrium_l1_max": float(same[both].max()) if both.any()
         else None,
+        "same_equilibrium_l1_median": float(np.median(same[both]))
+        if both.any() else None,
+        # the same distance in units of a damping time's worth of the
+        # stopping tolerance (the distance a run stopped by the rule may
+        # still have to go, for each of the two runs)
+        "same_equilibrium_per_damping_max": float(max(
+            same[i] / (test_in[i][2] * tol) for i in range(ntest)
+            if both[i])) if both.any() else None,
     }
+
+
+def experiment(ctx, n=256, spt=1000, ntrain=2048, ntest=128, iters=3000,
+               tol=1e-5, max_periods=300, seed=7, log=None, tol_train=None,
+               max_periods_train=None, report_damping=()):
+    """Train the correction on solver equilibria, then compare the periods
+    to equilibrium on held-out inputs from the Gaussian, from the
+    potential-well state alone and from the proposal (potential-well state
+    plus the learned correction).  The training equilibria may be
+    converged further than the judging tolerance (tol_train): the stopping
+    rule samples the profile once per synchrotron period and leaves
+    coherent oscillations of about a damping time's worth of the
+    tolerance, which would otherwise be learned as noise.  report_damping:
+    damping times (periods) with a held-out set of their own (S and g/R
+    drawn as before), reported under "at_damping"."""
+    rng = np.random.default_rng(seed)
+    train_in = sample_inputs(rng, ntrain, True)
+    test_in = sample_inputs(rng, ntest, False)
+    axes = bunch_params(n, spt, *train_in[0])["axes"]
+    dq = (axes[1] - axes[0]) / (n - 1)
+    # training targets: equilibrium (unit charge) minus potential well
+    tr_d, tr_p = equilibria(ctx, train_in, n, spt, tol_train or tol,
+                            max_periods_train or max_periods,
+                            start="potential_well")
+    tr_base = potential_well_states(ctx, train_in, n, spt)
+    ok = tr_p >= 0
+    resid = (simpson_normalise(tr_d[ok], dq).astype(np.float64)
+             - tr_base[ok]).reshape(int(ok.sum()), -1)
+    scale = float(resid.std()) or 1.0
+    x = normalise_inputs(*np.array(train_in)[ok].T)
+    tgt = (resid / scale).astype(np.float32)
+    net = WarmStartNet(ctx, n * n, seed=seed)
+    net.set_bias(tgt.mean(0))
+    hist = train(net, x, tgt, iters=iters)
+    out = {
+        "grid": n, "steps_per_period": spt, "tolerance_per_period": tol,
+        "train_tolerance_per_period": tol_train or tol, "iters": iters,
+        "damping_periods_domain": [TD_LO, TD_HI],
+        "train_samples": int(ntrain), "train_converged": int(ok.sum()),
+        "residual_scale": scale,
+        "train_loss_first": hist[0], "train_loss_last": hist[-1],
+    }
+    out.update(evaluate(ctx, net, test_in, scale, n, spt, tol, max_periods,
+                        dq))
+    if report_damping:
+        out["at_damping"] = {}
+        for td in report_damping:
+            held = sample_inputs(rng, ntest, False, damping=td)
+            out["at_damping"][str(td)] = evaluate(
+                ctx, net, held, scale, n, spt, tol, max_periods, dq)
     if log:
         log(out)
     return out, net
@@ -404,11 +460,15 @@ if __name__ == "__main__":
     ap.add_argument("--test", type=int, default=128)
     ap.add_argument("--iters", type=int, default=3000)
     ap.add_argument("--train-tol", type=float, default=None)
+    ap.add_argument("--max-periods", type=int, default=600)
+    ap.add_argument("--report-damping", type=float, nargs="*",
+                    default=[100.0])
     a = ap.parse_args()
     from . import build as _build
     _build.build()
     c = V.Context(0)
     res, _ = experiment(c, n=a.grid, spt=a.steps_per_period, ntrain=a.train,
                         ntest=a.test, iters=a.iters, tol_train=a.train_tol,
-                        max_periods_train=600)
+                        max_periods=a.max_periods, max_periods_train=600,
+                        report_damping=a.report_damping)
     print(json.dumps(res))
