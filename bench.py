@@ -100,7 +100,7 @@ def peaks():
 def traffic_per_cell():
     """DRAM bytes per cell-update of the step kernel from the committed ncu
     summary, if one exists."""
-    path = os.path.join(ROOT, "profiles", "k_bmaps0_scan256.json")
+    path = os.path.join(ROOT, "profiles", "k_bmaps0f_scan256.json")
     try:
         with open(path) as f:
             return float(json.load(f)["dram_bytes_per_cell"])
@@ -713,7 +713,9 @@ def main():
                      "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": 8 * cells,
                      "traffic": None if tpc is None else tpc * cells,
-                     "kernel": "k_bmaps0",
+                     "kernel": ("k_bmaps0f<128, 256>"
+                                if batch.kernel_tiles()["k_bmaps0f"] > 0
+                                else "k_bmaps0"),
                      "kernel_ms": ms_maps},
         "kernel_ms_per_step": kt,
         "continuous_value": continuous,
