@@ -44,7 +44,7 @@ using vfps::DevBuf;
 // ================================================================== host
 enum {
     TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_RINGF = 4,
-    TL_RINGF128 = 5, TL_RINGF64 = 6, TL_COUNT = 7
+    TL_RINGF128 = 5, TL_RINGF64 = 6, TL_RINGF512 = 7, TL_COUNT = 8
 };
 constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel, G = 2
 constexpr int RING4_N = 512;      // the mesh of the ring kernel, G = 4
@@ -56,11 +56,11 @@ struct vfps_batch {
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    // tile lists: TL_RINGF, TL_RINGF128, TL_RINGF64 (chain 0, n = 256,
-    // 128, 64, regular lattices: the fast
-    // ring kernel), TL_RING (the other chain-0 meshes up to 256 rows),
-    // TL_RING4 (chain 0, n = 512), TL_ROT (chain 1), TL_WIDE (chain 0,
-    // n = 1024)
+    // tile lists: TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512 (chain
+    // 0, n = 256, 128, 64, 512, regular lattices: the fast ring kernel),
+    // TL_RING (the other chain-0 meshes up to 256 rows), TL_RING4 (the
+    // other chain-0 meshes of 512 rows), TL_ROT (chain 1), TL_WIDE (chain
+    // 0, n = 1024)
     std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
     uint32_t max_n = 0;
@@ -88,8 +88,8 @@ struct vfps_batch {
     unsigned gridR = 0;        // persistent CTAs of k_bmaps0
     SmemR layoutR4{};          // the same for the 512-row ring kernel
     unsigned gridR4 = 0;
-    SmemR layoutRF[3] = {};    // the same for the fast ring kernel, per
-    unsigned gridRF[3] = {};   // mesh size 256, 128, 64
+    SmemR layoutRF[4] = {};    // the same for the fast ring kernel, per
+    unsigned gridRF[4] = {};   // mesh size 256, 128, 64, 512
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
@@ -234,8 +234,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     // that each fills the SMs the others leave free (no kernel's tail
     // idles the GPU); sequential when the kernels are timed one by one
     int classes = 0;
-    for (int c : {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RING, TL_RING4,
-                  TL_WIDE, TL_ROT}) {
+    for (int c : {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512, TL_RING,
+                  TL_RING4, TL_WIDE, TL_ROT}) {
         classes += b->htiles[c].empty() ? 0 : 1;
     }
     const bool forked = !ev && classes > 1;
@@ -277,6 +277,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
                 RTHREADS, b->layoutRF[1], (const RowInfo7*)b->rinfo7.p);
     ring_launch(k_bmaps0f<RTHREADS, 64>, TL_RINGF64, b->gridRF[2], RTHREADS,
                 b->layoutRF[2], (const RowInfo7*)b->rinfo7.p);
+    ring_launch(k_bmaps0f<RTHREADS, 512>, TL_RINGF512, b->gridRF[3],
+                RTHREADS, b->layoutRF[3], (const RowInfo7*)b->rinfo7.p);
     ring_launch(k_bmaps0<2, RTHREADS>, TL_RING, b->gridR, RTHREADS,
                 b->layoutR, (const RowInfo*)b->rinfo.p);
     ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
@@ -334,7 +336,8 @@ void build_tiles(vfps_batch* b, int tile_cells)
     int max_rows = 0;
     // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
-    int ring_rows = 0, ring_n = 0, ring4_rows = 0, ringf_rows[3] = {0, 0, 0};
+    int ring_rows = 0, ring_n = 0, ring4_rows = 0;
+    int ringf_rows[4] = {0, 0, 0, 0};
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
@@ -345,10 +348,16 @@ void build_tiles(vfps_batch* b, int tile_cells)
                                                 : (n == 128 ? TL_RINGF128
                                                             : TL_RINGF64))
                                     : TL_RING)
-                             : (n == RING4_N ? TL_RING4 : TL_WIDE));
+                             : (n == RING4_N ? ((B.flags & F_Y7)
+                                                    ? TL_RINGF512
+                                                    : TL_RING4)
+                                             : TL_WIDE));
+        const int fk = c == TL_RINGF ? 0
+                       : c == TL_RINGF128 ? 1
+                       : c == TL_RINGF64 ? 2
+                       : c == TL_RINGF512 ? 3 : -1;
         int tx = std::max(4, tile_cells / n);
-        if (c == TL_RING || c == TL_RING4 || c == TL_RINGF
-            || c == TL_RINGF128 || c == TL_RINGF64) {
+        if (c == TL_RING || c == TL_RING4 || fk >= 0) {
             // the ring holds two tiles with their halos: at most 32 staged
             // rows per tile keeps it at 64 slots or fewer
             tx = std::min(tx, std::max(4, 32 - B.halo_lo - B.halo_hi));
@@ -363,9 +372,8 @@ void build_tiles(vfps_batch* b, int tile_cells)
         if (c == TL_RING) {
             ring_rows = std::max(ring_rows, nr);
             ring_n = std::max(ring_n, n);
-        } else if (c == TL_RINGF || c == TL_RINGF128 || c == TL_RINGF64) {
-            const int k = c == TL_RINGF ? 0 : (c == TL_RINGF128 ? 1 : 2);
-            ringf_rows[k] = std::max(ringf_rows[k], nr);
+        } else if (fk >= 0) {
+            ringf_rows[fk] = std::max(ringf_rows[fk], nr);
         } else if (c == TL_RING4) {
             ring4_rows = std::max(ring4_rows, nr);
         } else if (c == TL_WIDE) {
@@ -385,7 +393,8 @@ void build_tiles(vfps_batch* b, int tile_cells)
         o = align16(o + bytes);
     };
     // the ring holds the staged rows of two tiles with their halos
-    auto ring_layout = [&](SmemR& L, int rows, int n, size_t rec) {
+    auto ring_layout = [&](SmemR& L, int rows, int n, size_t rec,
+                           bool halves = false) {
         const int rb = 2 * rows;
         L.rb = static_cast<uint32_t>(rb);
         L.rs = static_cast<uint32_t>(astride0(n));
@@ -393,26 +402,29 @@ void build_tiles(vfps_batch* b, int tile_cells)
         take(&L.ring, size_t(rb) * L.rs * 4);
         take(&L.s, size_t(rows) * rec);
         take(&L.tab, size_t(10) * n * 4);
+        take(&L.part, halves ? size_t(2) * rb * 4 : 0);
         take(&L.bar, 3 * sizeof(uint64_t));
         L.total = static_cast<uint32_t>(o);
         return o;
     };
-    const int flist[3] = {TL_RINGF, TL_RINGF128, TL_RINGF64};
-    const int fn[3] = {256, 128, 64};
-    for (int k = 0; k < 3; k++) {
+    const int flist[4] = {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512};
+    const int fn[4] = {256, 128, 64, 512};
+    for (int k = 0; k < 4; k++) {
         const int c = flist[k];
         if (b->htiles[c].empty()) {
             continue;
         }
         b->smem[c] = ring_layout(b->layoutRF[k], ringf_rows[k], fn[k],
-                                 sizeof(RowInfo7));
+                                 sizeof(RowInfo7), fn[k] > RING_MAX_N);
         const size_t nt = b->htiles[c].size();
         b->gridRF[k] =
             k == 0 ? persistent_grid(b, k_bmaps0f<RTHREADS, 256>, RTHREADS,
                                      b->smem[c], nt)
             : k == 1 ? persistent_grid(b, k_bmaps0f<RTHREADS, 128>, RTHREADS,
                                        b->smem[c], nt)
-                     : persistent_grid(b, k_bmaps0f<RTHREADS, 64>, RTHREADS,
+            : k == 2 ? persistent_grid(b, k_bmaps0f<RTHREADS, 64>, RTHREADS,
+                                       b->smem[c], nt)
+                     : persistent_grid(b, k_bmaps0f<RTHREADS, 512>, RTHREADS,
                                        b->smem[c], nt);
     }
     if (!b->htiles[TL_RING].empty()) {
@@ -476,6 +488,10 @@ void upload_tiles(vfps_batch* b)
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
                                        b->smem[TL_RINGF64], 1))));
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADS, 512>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_RINGF512], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<2, RTHREADS>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
@@ -977,7 +993,8 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                         tab.push_back(w5[size_t(y) * 5 + o]);
                     }
                 }
-                if (n <= RING_MAX_N && fast_ring_ok(dr, w5, n)
+                if ((n <= RING_MAX_N || n == RING4_N)
+                    && fast_ring_ok(dr, w5, n)
                     && !fast_ring_off()) {
                     B.flags |= F_Y7;
                 }
@@ -1537,7 +1554,8 @@ extern "C" int vfps_batch_kernel_tiles(const vfps_batch* b, uint32_t* tiles,
     }
     if (count > 0) {   // the fast ring kernel: every mesh size
         tiles[0] += static_cast<uint32_t>(b->htiles[TL_RINGF128].size()
-                                          + b->htiles[TL_RINGF64].size());
+                                          + b->htiles[TL_RINGF64].size()
+                                          + b->htiles[TL_RINGF512].size());
     }
     return VFPS_OK;
 }

@@ -1,5 +1,6 @@
 // k_bmaps0f: chain 0 (the reference's loop, src/main.cpp:1034-1044:
-// wake kick, RF kick, drift, Fokker-Planck) for meshes of 64..256 rows
+// wake kick, RF kick, drift, Fokker-Planck) for meshes of 64, 128, 256 and
+// 512 rows
 // whose lattice has the regular form of the benchmark's scans (checked on
 // the host, fast_ring_ok): every aligned group of 4 energy columns has one
 // drift shift, and the Fokker-Planck stencil of the lower half of the
@@ -21,6 +22,12 @@
 //           in packed FP32, Fokker-Planck with 4 taps (neighbour columns
 //           by shuffles), the new row to HBM and its Simpson sum; the row
 //           sums of 4 output rows leave in one reduce-scatter.
+// 512-row meshes: stage 1 gives a row to one warp (4 column groups per
+// lane); in stage 2 a pair of warps walks the rows, one warp per half of
+// the energy axis (two groups per lane, as a 256-row mesh), each warp
+// computing the drift of the two columns past its half that its
+// Fokker-Planck stencils reach; the two halves' row sums meet in shared
+// memory and are stored after the tile's next barrier.
 #pragma once
 
 namespace {
@@ -78,6 +85,18 @@ __device__ __forceinline__ float4 ykick7_checked(const float* row, int start,
     return make_float4(o[0], o[1], o[2], o[3]);
 }
 
+// ykick7 on G column groups STEP floats apart
+template <int AL, int G, int STEP>
+__device__ __forceinline__ void ykick7_groups(const float* src,
+                                              const float (&c)[7],
+                                              float4 (&o)[G])
+{
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        o[g] = ykick7<AL>(src + g * STEP, c);
+    }
+}
+
 // drift x-kick of 4 columns: tap j of the output reads window row r[j]
 // (packed FP32: two columns per instruction, each component rounded like
 // fmaf / a plain product)
@@ -97,6 +116,23 @@ __device__ __forceinline__ float4 drift4(const float4& r0, const float4& r1,
     hi = __ffma2_rn(make_float2(w[3].z, w[3].w), make_float2(r3.z, r3.w), hi);
     return make_float4(lo.x, lo.y, hi.x, hi.y);
 }
+
+// the same for 2 columns (the operations of drift4's first pair)
+__device__ __forceinline__ float2 drift2(const float2& r0, const float2& r1,
+                                         const float2& r2, const float2& r3,
+                                         const float2 (&w)[4])
+{
+    float2 v = __fmul2_rn(w[0], r0);
+    v = __ffma2_rn(w[1], r1, v);
+    v = __ffma2_rn(w[2], r2, v);
+    v = __ffma2_rn(w[3], r3, v);
+    return v;
+}
+
+template <int V>
+struct IntC {
+    static constexpr int value = V;
+};
 
 // Fokker-Planck of 4 columns with 4 taps: out[c] = sum_o F_o[c] w[c + o]
 // (w: the 7 drift values the taps reach, F_o: weight planes)
@@ -120,10 +156,10 @@ __device__ __forceinline__ float4 fp4(const float (&w)[7], const float4& f0,
     return make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// N: the mesh size of every bunch of the tile list (64, 128 or 256; the
-// lane mapping, strides and shuffle widths are constants)
+// N: the mesh size of every bunch of the tile list (64, 128, 256 or 512;
+// the lane mapping, strides and shuffle widths are constants)
 template <int NT, int N>
-__global__ void __launch_bounds__(NT, 3)
+__global__ void __launch_bounds__(NT, N > 256 ? 2 : 3)
 k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
           uint32_t ntiles, const float* __restrict__ tabs,
           const float* __restrict__ dwt, const RowInfo7* __restrict__ rinfo,
@@ -136,6 +172,8 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     RowInfo7* S = reinterpret_cast<RowInfo7*>(base + L.s);
     float* T = reinterpret_cast<float*>(base + L.tab);
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
+    // 512 rows: the halves' row sums of a tile, [2 tiles][2 halves][rb/2]
+    float* part = reinterpret_cast<float*>(base + L.part);
     const int rb = int(L.rb);
     constexpr int rs = N + 2 * APAD + 16;   // astride0(N), the ring's L.rs
     const int ring_floats = rb * rs;
@@ -202,13 +240,24 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                    false, true);
     }
     int bad = 0;
+    constexpr bool HALF = N > 256;
+    // the previous tile's row sums (512 rows): stored after a barrier
+    int prev_off = 0, prev_rows = 0;
+    float prev_h03 = 0.f;
+    auto store_halves = [&](int buf) {
+        const float* p0 = part + buf * rb;
+        for (int i = threadIdx.x; i < prev_rows; i += NT) {
+            pout[prev_off + i] = prev_h03 * (p0[i] + p0[i + (rb >> 1)]);
+        }
+    };
     for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
         const Tile t = tiles[tid];
         const BDev B = bd[t.bunch];
         constexpr int n = N;
         const int x0 = int(t.x0);
         const int rows = int(t.rows);
-        constexpr int seg = N >> 3;          // lanes per row
+        constexpr int G1 = HALF ? 4 : 2;     // column groups per lane
+        constexpr int seg = N / (4 * G1);    // lanes per row (stage 1)
         const int l = threadIdx.x & (seg - 1);
         const int rl = threadIdx.x / seg;    // segment
         constexpr int rp = NT / seg;         // segments
@@ -236,41 +285,47 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                     const int s = __float_as_int(q0.x);
                     const float c[7] = {q0.y, q0.z, q0.w, q1.x, q1.y, q1.z,
                                         q1.w};
-                    float4 oA, oB;
+                    // lane l's groups start at 4l + g n/G1
+                    constexpr int STEP = N / G1;
+                    float4 o[G1];
                     // the window of every lane inside the staged row: the
                     // lowest starts at APAD + s, the highest ends 16 floats
                     // after its aligned start APAD + n - 4 + (s & ~3)
                     if (s >= -APAD && s <= APAD + 7) {
-                        const float* wa = row + APAD + (s & ~3) + yA;
-                        const float* wb = row + APAD + (s & ~3) + yB;
+                        const float* w0 = row + APAD + (s & ~3) + yA;
                         switch (s & 3) {
                         case 0:
-                            oA = ykick7<0>(wa, c);
-                            oB = ykick7<0>(wb, c);
+                            ykick7_groups<0, G1, STEP>(w0, c, o);
                             break;
                         case 1:
-                            oA = ykick7<1>(wa, c);
-                            oB = ykick7<1>(wb, c);
+                            ykick7_groups<1, G1, STEP>(w0, c, o);
                             break;
                         case 2:
-                            oA = ykick7<2>(wa, c);
-                            oB = ykick7<2>(wb, c);
+                            ykick7_groups<2, G1, STEP>(w0, c, o);
                             break;
                         default:
-                            oA = ykick7<3>(wa, c);
-                            oB = ykick7<3>(wb, c);
+                            ykick7_groups<3, G1, STEP>(w0, c, o);
                             break;
                         }
                     } else {
-                        oA = ykick7_checked(row, APAD + yA + s, as, c);
-                        oB = ykick7_checked(row, APAD + yB + s, as, c);
+#pragma unroll
+                        for (int g = 0; g < G1; g++) {
+                            o[g] = ykick7_checked(row, APAD + yA + g * STEP
+                                                  + s, as, c);
+                        }
                     }
                     __syncwarp(rmask);
-                    *reinterpret_cast<float4*>(row + APAD + yA) = oA;
-                    *reinterpret_cast<float4*>(row + APAD + yB) = oB;
+#pragma unroll
+                    for (int g = 0; g < G1; g++) {
+                        *reinterpret_cast<float4*>(row + APAD + yA
+                                                   + g * STEP) = o[g];
+                    }
                 } else {
-                    *reinterpret_cast<float4*>(row + APAD + yA) = z;
-                    *reinterpret_cast<float4*>(row + APAD + yB) = z;
+#pragma unroll
+                    for (int g = 0; g < G1; g++) {
+                        *reinterpret_cast<float4*>(row + APAD + yA
+                                                   + g * (N / G1)) = z;
+                    }
                 }
             }
         }
@@ -286,6 +341,11 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 mbar_wait_bounded(&bar[2], tab_ph, WAIT_NS);
             }
             break;
+        }
+        if constexpr (HALF) {
+            if (k > 0) {
+                store_halves((k - 1) & 1);
+            }
         }
 
         // stage the next tile's new rows: their slots hold no row that this
@@ -328,7 +388,7 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         // walks output rows [ra, ra + per) of the tile in steps of 4 (every
         // segment makes the same number of steps, so the shuffles see whole
         // warps; rows past the tile are computed and dropped)
-        {
+        if constexpr (!HALF) {
             const float* W = T;             // drift weights [4][n], shift [n]
             const float* F = T + 5 * n;     // Fokker-Planck planes [5][n]
             const float h03 = tabs[B.tab_off + TAB_WS * n];
@@ -462,10 +522,210 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 const float p3 = one(X + 3, a3, a0, a1, a2, b3, b0, b1, b2);
                 flush(X, p0, p1, p2, p3);
             }
+        } else {
+            // a pair of warps per run of output rows: warp h of the pair
+            // takes columns [h n/2, (h + 1) n/2), its lane l the groups at
+            // h n/2 + 4l (A) and h n/2 + n/4 + 4l (B); both groups of the
+            // lower half take the stencil's lower form (offsets -2..1,
+            // planes 0..3), those of the upper half the upper form (-1..2,
+            // planes 1..4).  The columns past the half that the stencils
+            // reach (n/2, n/2 + 1 below; n/2 - 1 above) come from a third,
+            // 2-column window (C) of the same rows
+            const float* W = T;
+            const float* F = T + 5 * n;
+            const float h03 = tabs[B.tab_off + TAB_WS * n];
+            const int h = rl & 1;
+            constexpr int pairs = rp >> 1;
+            const int per = (rows + pairs - 1) / pairs;
+            const int ra = (rl >> 1) * per;
+            const int xend = x0 + min(rows, ra + per);
+            float* psum = part + (k & 1) * rb + h * (rb >> 1) - x0;
+            auto slot0 = [&](int x) {
+                int q = (x + mc.off) % rb;
+                return q < 0 ? q + rb : q;
+            };
+            auto next = [&](int& o) {
+                o += rs;
+                o -= o >= ring_floats ? ring_floats : 0;
+            };
+            const bool first = l == 0, last = l == 31;
+            const int lm = (l + 31) & 31, lp = (l + 1) & 31;
+            float* obase = dout + B.dens_off;
+            auto walk = [&](auto hc) {
+                constexpr int H = decltype(hc)::value;
+                constexpr int P0 = H;           // first Fokker-Planck plane
+                const int yA = H * (n >> 1) + 4 * l;
+                const int yB = yA + (n >> 2);
+                constexpr int yC = H == 0 ? (n >> 1) : (n >> 1) - 2;
+                const int shA = __float_as_int(W[4 * n + yA]);
+                const int shB = __float_as_int(W[4 * n + yB]);
+                const int shC = __float_as_int(W[4 * n + yC]);
+                float4 wA[4], wB[4];
+                float2 wC[4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    wA[j] = *reinterpret_cast<const float4*>(W + j * n + yA);
+                    wB[j] = *reinterpret_cast<const float4*>(W + j * n + yB);
+                    wC[j] = *reinterpret_cast<const float2*>(W + j * n + yC);
+                }
+                auto fw = [&](int o, int y) {
+                    return *reinterpret_cast<const float4*>(F + o * n + y);
+                };
+                int oA = slot0(x0 + ra + shA) * rs + APAD + yA;
+                int oB = slot0(x0 + ra + shB) * rs + APAD + yB;
+                int oC = slot0(x0 + ra + shC) * rs + APAD + yC;
+                float4 a0, a1, a2, a3, b0, b1, b2, b3;
+                float2 c0, c1, c2, c3;
+                a0 = *reinterpret_cast<const float4*>(ring + oA);
+                b0 = *reinterpret_cast<const float4*>(ring + oB);
+                c0 = *reinterpret_cast<const float2*>(ring + oC);
+                next(oA);
+                next(oB);
+                next(oC);
+                a1 = *reinterpret_cast<const float4*>(ring + oA);
+                b1 = *reinterpret_cast<const float4*>(ring + oB);
+                c1 = *reinterpret_cast<const float2*>(ring + oC);
+                next(oA);
+                next(oB);
+                next(oC);
+                a2 = *reinterpret_cast<const float4*>(ring + oA);
+                b2 = *reinterpret_cast<const float4*>(ring + oB);
+                c2 = *reinterpret_cast<const float2*>(ring + oC);
+                next(oA);
+                next(oB);
+                next(oC);
+                // offset +2 of the lower half: zero but in its last column
+                // n/2 - 1 (the last lane's 4th of B), whose neighbour
+                // n/2 + 1 is C's second column
+                const float f4b = H == 0 ? F[4 * n + yB + 3] : 0.f;
+                auto one = [&](int X, const float4& r0, const float4& r1,
+                               const float4& r2, float4& r3, const float4& s0,
+                               const float4& s1, const float4& s2, float4& s3,
+                               const float2& t0, const float2& t1,
+                               const float2& t2, float2& t3) {
+                    r3 = *reinterpret_cast<const float4*>(ring + oA);
+                    s3 = *reinterpret_cast<const float4*>(ring + oB);
+                    t3 = *reinterpret_cast<const float2*>(ring + oC);
+                    next(oA);
+                    next(oB);
+                    next(oC);
+                    const float4 dA = drift4(r0, r1, r2, r3, wA);
+                    const float4 dB = drift4(s0, s1, s2, s3, wB);
+                    const float2 dC = drift2(t0, t1, t2, t3, wC);
+                    float4 fA, fB;
+                    if constexpr (H == 0) {
+                        // A: left lane l-1's A2, A3 (lane 0: lane 31's,
+                        // meeting the zero stencils of columns 0, 1), right
+                        // lane l+1's A0 (lane 31: lane 0's B0); B: left
+                        // lane l-1's B2, B3 (lane 0: lane 31's A2, A3),
+                        // right lane l+1's B0 (lane 31: C's first column)
+                        const float aL2 = __shfl_sync(0xffffffffu, dA.z, lm);
+                        const float aL3 = __shfl_sync(0xffffffffu, dA.w, lm);
+                        const float aR0 = __shfl_sync(0xffffffffu, dA.x, lp);
+                        const float bL2 = __shfl_sync(0xffffffffu, dB.z, lm);
+                        const float bL3 = __shfl_sync(0xffffffffu, dB.w, lm);
+                        const float bR0 = __shfl_sync(0xffffffffu, dB.x, lp);
+                        const float wa[7] = {aL2, aL3, dA.x, dA.y, dA.z, dA.w,
+                                             last ? bR0 : aR0};
+                        const float wb[7] = {first ? aL2 : bL2,
+                                             first ? aL3 : bL3, dB.x, dB.y,
+                                             dB.z, dB.w, last ? dC.x : bR0};
+                        fA = fp4(wa, fw(P0, yA), fw(P0 + 1, yA),
+                                 fw(P0 + 2, yA), fw(P0 + 3, yA));
+                        fB = fp4(wb, fw(P0, yB), fw(P0 + 1, yB),
+                                 fw(P0 + 2, yB), fw(P0 + 3, yB));
+                        fB.w = fmaf(f4b, dC.y, fB.w);
+                    } else {
+                        // A: left lane l-1's A3 (lane 0: C's second
+                        // column), right lane l+1's A0, A1 (lane 31: lane
+                        // 0's B0, B1); B: left lane l-1's B3 (lane 0: lane
+                        // 31's A3), right lane l+1's B0, B1 (lane 31: lane
+                        // 0's, meeting the zero stencils of columns n-2,
+                        // n-1)
+                        const float aL3 = __shfl_sync(0xffffffffu, dA.w, lm);
+                        const float aR0 = __shfl_sync(0xffffffffu, dA.x, lp);
+                        const float aR1 = __shfl_sync(0xffffffffu, dA.y, lp);
+                        const float bL3 = __shfl_sync(0xffffffffu, dB.w, lm);
+                        const float bR0 = __shfl_sync(0xffffffffu, dB.x, lp);
+                        const float bR1 = __shfl_sync(0xffffffffu, dB.y, lp);
+                        const float wa[7] = {first ? dC.y : aL3, dA.x, dA.y,
+                                             dA.z, dA.w, last ? bR0 : aR0,
+                                             last ? bR1 : aR1};
+                        const float wb[7] = {first ? aL3 : bL3, dB.x, dB.y,
+                                             dB.z, dB.w, bR0, bR1};
+                        fA = fp4(wa, fw(P0, yA), fw(P0 + 1, yA),
+                                 fw(P0 + 2, yA), fw(P0 + 3, yA));
+                        fB = fp4(wb, fw(P0, yB), fw(P0 + 1, yB),
+                                 fw(P0 + 2, yB), fw(P0 + 3, yB));
+                    }
+                    if (X < xend) {
+                        float* o = obase + size_t(X) * n;
+                        *reinterpret_cast<float4*>(o + yA) = fA;
+                        *reinterpret_cast<float4*>(o + yB) = fB;
+                    }
+                    // Simpson weights: even columns 2, odd 4, columns 0
+                    // and n - 1 one
+                    float e = (fA.x + fA.z) + (fB.x + fB.z);
+                    float od = (fA.y + fA.w) + (fB.y + fB.w);
+                    if (H == 0 && first) {
+                        e -= 0.5f * fA.x;
+                    }
+                    if (H == 1 && last) {
+                        od -= 0.75f * fB.w;
+                    }
+                    return fmaf(4.f, od, 2.f * e);
+                };
+                // the half's sums of 4 output rows: reduce-scatter over
+                // the warp, one lane stores a row's
+                auto flush = [&](int X, float p0, float p1, float p2,
+                                 float p3) {
+                    const bool u1 = (l & 16) != 0;
+                    float k0 = u1 ? p2 : p0, k1 = u1 ? p3 : p1;
+                    const float s0 = u1 ? p0 : p2, s1 = u1 ? p1 : p3;
+                    k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+                    k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+                    const bool u2 = (l & 8) != 0;
+                    float v = u2 ? k1 : k0;
+                    v += __shfl_xor_sync(0xffffffffu, u2 ? k0 : k1, 8);
+                    v += __shfl_xor_sync(0xffffffffu, v, 4);
+                    v += __shfl_xor_sync(0xffffffffu, v, 2);
+                    v += __shfl_xor_sync(0xffffffffu, v, 1);
+                    const int r = (u1 ? 2 : 0) + (u2 ? 1 : 0);
+                    if ((l & 7) == 0 && X + r < xend) {
+                        psum[X + r] = v;
+                    }
+                };
+                for (int X = x0 + ra; X < x0 + ra + per; X += 4) {
+                    const float p0 = one(X, a0, a1, a2, a3, b0, b1, b2, b3,
+                                         c0, c1, c2, c3);
+                    const float p1 = one(X + 1, a1, a2, a3, a0, b1, b2, b3,
+                                         b0, c1, c2, c3, c0);
+                    const float p2 = one(X + 2, a2, a3, a0, a1, b2, b3, b0,
+                                         b1, c2, c3, c0, c1);
+                    const float p3 = one(X + 3, a3, a0, a1, a2, b3, b0, b1,
+                                         b2, c3, c0, c1, c2);
+                    flush(X, p0, p1, p2, p3);
+                }
+            };
+            if (h == 0) {
+                walk(IntC<0>{});
+            } else {
+                walk(IntC<1>{});
+            }
+            prev_off = int(B.prof_off) + x0;
+            prev_rows = rows;
+            prev_h03 = h03;
         }
         mc = mn;
         lo_c = lo_n;
         hi_c = hi_n;
+    }
+    if constexpr (HALF) {
+        // the last tile's row sums (after a wait that ran out, none)
+        bad = __syncthreads_or(bad);
+        if (!bad && prev_rows > 0) {
+            store_halves((t_end - t_begin - 1) & 1);
+        }
     }
     if (bad && threadIdx.x == 0) {
         atomicCAS(status, 0, VFPS_ERR_TIMEOUT);

@@ -363,3 +363,53 @@ def test_fast_ring_kernel(gpu_ctx, monkeypatch):
     odd = make_batch(gpu_ctx, [(p, 0, p["Ib"], 4, False)], {n: z})
     tiles = odd.kernel_tiles()
     assert tiles["k_bmaps0f"] == 0 and tiles["k_bmaps0"] > 0, tiles
+
+
+def test_fast_ring_kernel_512(gpu_ctx, monkeypatch):
+    """512-row meshes on the lattices of the bursting and uneven workloads
+    (4000 and 2000 steps per period, g/R = 0.006, resistive wall; orders
+    2..4) run on the fast ring kernel's half-row form (a pair of warps per
+    output row, the halves' row sums joined in shared memory).  Against the
+    classic 512-row ring kernel: density and profile within 2e-5 relative
+    L1 after 40 steps; against FP64: the bar; the profile against the FP64
+    Simpson sums of the same density rows (relative L1 <= 1e-6, largest
+    row error <= 1e-5 of the peak)."""
+    n = 512
+    gap = 0.006 * P.derive(GridSize=n, StepsPerTs=4000, padding=2.0)["R_bend"]
+    specs = []
+    for spt, S, it in ((4000, 0.8, 4), (4000, 1.6, 4), (2000, 0.3, 2),
+                       (2000, 1.2, 3)):
+        p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=gap,
+                     S_csr=S, WallConductivity=5.8e7)
+        specs.append((p, 0, p["Ib"], it, False))
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(specs[0][0]))
+    steps = 40
+    fast = make_batch(gpu_ctx, specs, {n: z})
+    tiles = fast.kernel_tiles()
+    assert tiles["k_bmaps0f"] > 0 and tiles["k_bmaps0<4>"] == 0, tiles
+    fast.step(steps)
+    monkeypatch.setenv("VFPS_RING_KERNEL", "classic")
+    classic = make_batch(gpu_ctx, specs, {n: z})
+    tiles = classic.kernel_tiles()
+    assert tiles["k_bmaps0f"] == 0 and tiles["k_bmaps0<4>"] > 0, tiles
+    classic.step(steps)
+    monkeypatch.delenv("VFPS_RING_KERNEL")
+    assert gpu_ctx.device_status() == 0
+    a, b = fast.download(), classic.download()
+    ws = np.asarray(oracle.simpson(n, specs[0][0]["axes"][0],
+                                   specs[0][0]["axes"][1], np.float32),
+                    np.float64)
+    for i, (p, ch, ib, it, cl) in enumerate(specs):
+        off, _ = fast.layout(i)
+        ga = a[off:off + n * n].reshape(n, n)
+        gb = b[off:off + n * n].reshape(n, n)
+        assert rel_l1(ga, gb) <= 2e-5, i
+        assert rel_l1(fast.profile(i), classic.profile(i)) <= 2e-5, i
+        sums = ga.astype(np.float64) @ ws
+        prof = np.asarray(fast.profile(i), np.float64)
+        assert np.abs(prof - sums).sum() / np.abs(sums).sum() <= 1e-6, i
+        assert np.abs(prof - sums).max() <= 1e-5 * sums.max(), i
+        ref = oracle_sim(p, ch, ib, z.data(), it=it, clamp=cl)
+        ref.step(steps)
+        assert rel_l1(ga, ref.density(0)) <= TOL, i
+        assert rel_l1(fast.profile(i), ref.profile(0)) <= TOL, i

@@ -38,14 +38,17 @@ EMPTY = []   # (bunch, lo, hi) of continuation tiles staging no mesh row
 
 def window_walk(bunches, b, x0, rows, rb, off, ring, nthreads=128):
     """Stage 2 of k_bmaps0f (inovesa_gb300/csrc/ring_fast.cuh) on one
-    tile: every segment of n/8 lanes walks its run of output rows in steps
-    of 4 with a window of 4 staged rows per column group, the window's
-    ring offset advanced one slot per row from a start reduced modulo the
-    ring.  For every drift shift the mesh can have, the rows a valid output
-    row reads must be in the slots the walk loads (and every load must stay
-    inside the ring, also for rows past the tile)."""
+    tile: every segment of n/8 lanes (512 rows: a pair of warps, one per
+    half of the row) walks its run of output rows in steps of 4 with a
+    window of 4 staged rows per column group, the window's ring offset
+    advanced one slot per row from a start reduced modulo the ring.  For
+    every drift shift the mesh can have, the rows a valid output row reads
+    must be in the slots the walk loads (and every load must stay inside
+    the ring, also for rows past the tile); the halves' row sums of a
+    512-row tile fit their buffer of rb/2 rows."""
     n, hlo, hhi = bunches[b]
     seg = n // 8
+    assert rows <= rb // 2
     rp = nthreads // seg
     per = -(-rows // rp)
     steps = -(-per // 4) * 4
@@ -155,7 +158,7 @@ def test_ring_staging_invariants(mix, tile_cells):
 
 
 @pytest.mark.parametrize("mix", ["scan 256", "narrow halos", "wide halos",
-                                 "short tails"])
+                                 "512 rows", "short tails"])
 @pytest.mark.parametrize("tile_cells", [2048, 4096, 8192])
 def test_fast_ring_windows(mix, tile_cells):
     bunches = MIXES[mix]
