@@ -6,6 +6,7 @@
 //  k_kick_y    KickMap y-kick, one CTA per mesh row (src/SM/KickMap.cpp:244-266)
 //  k_kick_x    KickMap x-kick (src/SM/KickMap.cpp:221-242)
 //  k_fp        FokkerPlanckMap::apply (src/SM/FokkerPlanckMap.cpp:170-213)
+#include <algorithm>
 #include <cfloat>
 
 #include "vfps_internal.cuh"
@@ -139,6 +140,208 @@ __global__ void k_fp(const float* __restrict__ in, float* __restrict__ out,
     out[row + y] = value;
 }
 
+// ------------------------------------------------ row-sweep forms
+// Meshes whose side is a multiple of 4 (up to PLAIN_V4_MAX) take these
+// instead of the thread-per-cell kernels above: 16-byte row sweeps in and
+// out, the stencils computed once per thread for its 4 columns and kept
+// in registers, and rows staged in shared memory where a stencil reads
+// along the row.  Every output is the same sum in the same order as the
+// kernels above; a tap outside the mesh reads a zero pad instead of being
+// skipped, and adds fmul(0, w) = +-0 (an exact no-op, because the sum is
+// never -0).
+
+// one output group: taps j < it of the aligned window v (AL: offset of
+// the first tap of the first output)
+template <int AL>
+__device__ __forceinline__ float4 kick_row4(const float4 (&v4)[3],
+                                            const float (&w)[4], int it)
+{
+    const float v[12] = {v4[0].x, v4[0].y, v4[0].z, v4[0].w,
+                         v4[1].x, v4[1].y, v4[1].z, v4[1].w,
+                         v4[2].x, v4[2].y, v4[2].z, v4[2].w};
+    float o[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        float value = 0.f;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (j < it) {
+                value = fadd(value, fmul(v[AL + c + j], w[j]));
+            }
+        }
+        o[c] = value;
+    }
+    return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// y-kick, one CTA per (bunch, row): the row in shared memory between zero
+// pads of kick_pad(n) floats (a valid tap lies at most n/2 + 3 columns
+// away), the stencil uniform over the row, 4 outputs per thread from 3
+// aligned 16-byte reads (the window's alignment is the same for the whole
+// row)
+__host__ __device__ inline int kick_pad(uint32_t n)
+{
+    return int(((n / 2 + 3) & ~3u) + 16);
+}
+
+__global__ void k_kick_y4(const float* __restrict__ in,
+                          float* __restrict__ out,
+                          const float* __restrict__ offsets, uint32_t n,
+                          int it)
+{
+    extern __shared__ float4 row4[];
+    const uint32_t row = blockIdx.x;
+    const KickStencil s = kick_stencil(offsets[row], n, it);
+    const int pad4 = kick_pad(n) / 4, n4 = int(n / 4);
+    const float4* src = reinterpret_cast<const float4*>(in + size_t(row) * n);
+    float4* dst = reinterpret_cast<float4*>(out + size_t(row) * n);
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool any = s.valid[0] || s.valid[1] || s.valid[2] || s.valid[3];
+    if (!any) {   // no tap inside the mesh: the row is zero
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+            dst[i] = z;
+        }
+        return;
+    }
+    for (int i = threadIdx.x; i < 2 * pad4 + n4; i += blockDim.x) {
+        const int k = i - pad4;
+        row4[i] = (k >= 0 && k < n4) ? __ldg(src + k) : z;
+    }
+    __syncthreads();
+    // shift[0] lies in [-n/2 - 3, n/2): every window inside the pads
+    const int s0 = s.shift[0];
+    const int al = s0 & 3;
+    const int b4 = pad4 + ((s0 - al) >> 2);
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+        const float4 v[3] = {row4[b4 + i], row4[b4 + i + 1],
+                             row4[b4 + i + 2]};
+        float4 o;
+        switch (al) {
+        case 0: o = kick_row4<0>(v, s.w, it); break;
+        case 1: o = kick_row4<1>(v, s.w, it); break;
+        case 2: o = kick_row4<2>(v, s.w, it); break;
+        default: o = kick_row4<3>(v, s.w, it); break;
+        }
+        dst[i] = o;
+    }
+}
+
+// x-kick: a CTA per block of rows of one bunch; each thread owns 4
+// columns (their stencils, one per column, in registers for the block)
+// and sweeps the rows with 16-byte reads where the 4 columns take the
+// same shifts, column by column otherwise
+constexpr int KICKX_ROWS = 8;
+
+__global__ void k_kick_x4(const float* __restrict__ in,
+                          float* __restrict__ out,
+                          const float* __restrict__ offsets, uint32_t n,
+                          int it)
+{
+    const int n4 = int(n / 4);
+    const size_t nxy = size_t(n) * n;
+    const float* src = in + blockIdx.y * nxy;
+    float* dst = out + blockIdx.y * nxy;
+    const int xa = blockIdx.x * KICKX_ROWS;
+    const int xe = min(int(n), xa + KICKX_ROWS);
+    for (int g = threadIdx.x; g < n4; g += blockDim.x) {
+        KickStencil s[4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            s[c] = kick_stencil(offsets[4 * g + c], n, it);
+        }
+        bool same = true;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            same = same && s[1].shift[j] == s[0].shift[j]
+                   && s[2].shift[j] == s[0].shift[j]
+                   && s[3].shift[j] == s[0].shift[j];
+        }
+        for (int x = xa; x < xe; x++) {
+            float o[4] = {0.f, 0.f, 0.f, 0.f};
+            if (same) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int xs = x + s[0].shift[j];
+                    if (j < it && xs >= 0 && xs < int(n)) {
+                        const float4 v = __ldg(reinterpret_cast<const float4*>(
+                            src + size_t(xs) * n) + g);
+                        o[0] = fadd(o[0], fmul(v.x, s[0].w[j]));
+                        o[1] = fadd(o[1], fmul(v.y, s[1].w[j]));
+                        o[2] = fadd(o[2], fmul(v.z, s[2].w[j]));
+                        o[3] = fadd(o[3], fmul(v.w, s[3].w[j]));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        const int xs = x + s[c].shift[j];
+                        if (j < it && xs >= 0 && xs < int(n)) {
+                            o[c] = fadd(o[c], fmul(__ldg(src + size_t(xs) * n
+                                                         + 4 * g + c),
+                                                   s[c].w[j]));
+                        }
+                    }
+                }
+            }
+            reinterpret_cast<float4*>(dst + size_t(x) * n)[g] =
+                make_float4(o[0], o[1], o[2], o[3]);
+        }
+    }
+}
+
+// Fokker-Planck: a CTA per block of rows of one bunch, the rows staged in
+// shared memory by 16-byte reads; each thread owns 4 columns, whose
+// stencils (ip <= 4 taps: column index and weight) it loads once
+__global__ void k_fp4(const float* __restrict__ in, float* __restrict__ out,
+                      const uint32_t* __restrict__ idx,
+                      const float* __restrict__ w, uint32_t n, int ip,
+                      int rows)
+{
+    extern __shared__ float4 blk4[];
+    const float* blk = reinterpret_cast<const float*>(blk4);
+    const int n4 = int(n / 4);
+    const int xa = blockIdx.x * rows;
+    const int nr = min(int(n) - xa, rows);
+    const size_t base = (blockIdx.y * size_t(n) + xa) * n;
+    const float4* src = reinterpret_cast<const float4*>(in + base);
+    for (int i = threadIdx.x; i < nr * n4; i += blockDim.x) {
+        blk4[i] = __ldg(src + i);
+    }
+    __syncthreads();
+    float4* dst = reinterpret_cast<float4*>(out + base);
+    for (int g = threadIdx.x; g < n4; g += blockDim.x) {
+        uint32_t ix[4][4];
+        float wt[4][4];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const size_t k = size_t(4 * g + c) * ip + j;
+                ix[c][j] = j < ip ? idx[k] : 0u;
+                wt[c][j] = j < ip ? w[k] : 0.f;
+            }
+        }
+        for (int r = 0; r < nr; r++) {
+            const float* rowp = blk + size_t(r) * n;
+            float o[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                float value = 0.f;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    if (j < ip) {
+                        value = fadd(value, fmul(rowp[ix[c][j]], wt[c][j]));
+                    }
+                }
+                o[c] = value;
+            }
+            dst[size_t(r) * n4 + g] = make_float4(o[0], o[1], o[2], o[3]);
+        }
+    }
+}
+
 // DynamicRFKickMap::apply (src/SM/DynamicRFKickMap.cpp:79-109 and
 // RFKickMap::_calcKick, src/SM/RFKickMap.cpp:59-83): the modulation of
 // apply number `step` -- phase = syncphase + N(0,1) phasenoise + modampl
@@ -219,11 +422,31 @@ void launch_rotation(const vfps_map* m)
     VFPS_LAUNCHED();
 }
 
+// the row-sweep forms: sides that are a multiple of 4, up to this size
+// (shared memory of the y-kick's padded row and of k_fp4's rows: 32 KiB at
+// most, within the default limit)
+constexpr uint32_t PLAIN_V4_MAX = 4096;
+
+bool plain_v4(uint32_t n)
+{
+    return n % 4 == 0 && n <= PLAIN_V4_MAX;
+}
+
 void launch_kick(const vfps_map* m, const float* offset)
 {
     const vfps_ps* in = m->in;
     const uint32_t n = in->n;
-    if (m->axis == VFPS_AXIS_Y) {
+    const int t4 = int(std::min<uint32_t>(256, ((n / 4 + 31) / 32) * 32));
+    const bool v4 = plain_v4(n) && !m->cells;
+    if (v4 && m->axis == VFPS_AXIS_Y) {
+        const size_t smem = (2 * size_t(kick_pad(n)) + n) * sizeof(float);
+        k_kick_y4<<<in->nb * n, t4, smem, in->ctx->stream>>>(
+            in->data.p, m->out->data.p, offset, n, m->it);
+    } else if (v4) {
+        dim3 grid((n + KICKX_ROWS - 1) / KICKX_ROWS, in->nb);
+        k_kick_x4<<<grid, t4, 0, in->ctx->stream>>>(
+            in->data.p, m->out->data.p, offset, n, m->it);
+    } else if (m->axis == VFPS_AXIS_Y) {
         const int threads = n >= 256 ? 256 : ((n + 31) / 32) * 32;
         k_kick_y<<<in->nb * n, threads, 0, in->ctx->stream>>>(
             in->data.p, m->out->data.p, offset, n, m->it);
@@ -239,6 +462,18 @@ void launch_fp(const vfps_map* m)
 {
     const vfps_ps* in = m->in;
     const uint32_t n = in->n;
+    if (plain_v4(n) && m->ip <= 4 && !m->cells) {
+        // 8 rows of up to 1024 floats (32 KiB), fewer for wider meshes
+        const int rows = int(std::max<uint32_t>(1, std::min<uint32_t>(
+            8, 8192 / n)));
+        const int t4 = int(std::min<uint32_t>(256, ((n / 4 + 31) / 32) * 32));
+        dim3 grid((n + rows - 1) / rows, in->nb);
+        k_fp4<<<grid, t4, size_t(rows) * n * sizeof(float),
+                in->ctx->stream>>>(in->data.p, m->out->data.p, m->fp_idx.p,
+                                   m->fp_w.p, n, m->ip, rows);
+        VFPS_LAUNCHED();
+        return;
+    }
     dim3 grid((n + 127) / 128, n, in->nb);
     k_fp<<<grid, 128, 0, in->ctx->stream>>>(in->data.p, m->out->data.p,
                                             m->fp_idx.p, m->fp_w.p, n, m->ip);

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -170,8 +171,18 @@ struct DynRf {
     uint32_t seed = 0;
 };
 
+// VFPS_PLAIN_KERNEL=cell keeps a plain kick or Fokker-Planck map created
+// while it is set on the thread-per-cell kernels (the row-sweep forms and
+// these side by side in tests)
+inline bool plain_cells_env()
+{
+    const char* v = std::getenv("VFPS_PLAIN_KERNEL");
+    return v && std::string(v) == "cell";
+}
+
 struct vfps_map {
     MapKind kind = MAP_IDENTITY;
+    bool cells = plain_cells_env();
     int device = 0;
     vfps_ps* in = nullptr;
     vfps_ps* out = nullptr;
@@ -335,7 +346,7 @@ __device__ __forceinline__ KickStencil kick_stencil(float offset, uint32_t n,
 {
     KickStencil s;
     const float poffs = fadd(static_cast<float>(n / 2), offset);
-    int jd;
+    int jd = 0;   // no valid tap when base_index fails
     float f;
     const bool ok = base_index(poffs, n, &jd, &f);
     float c[4] = {0.f, 0.f, 0.f, 0.f};
