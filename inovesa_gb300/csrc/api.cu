@@ -1038,6 +1038,20 @@ extern "C" int vfps_fokker_planck_map_create(vfps_ps* in, vfps_ps* out,
         m->fp_w.alloc(w.size());
         h2d(m->fp_idx.p, idx.data(), idx.size(), in->ctx);
         h2d(m->fp_w.p, w.data(), w.size(), in->ctx);
+        // the same tables tap-major [4][n] (a missing 4th tap: index 0,
+        // weight 0) for the row-sweep kernel's 16-byte reads
+        std::vector<uint32_t> it4(size_t(4) * n, 0u);
+        std::vector<float> wt4(size_t(4) * n, 0.f);
+        for (uint32_t y = 0; y < n; y++) {
+            for (int k = 0; k < derivation; k++) {
+                it4[size_t(k) * n + y] = idx[size_t(y) * derivation + k];
+                wt4[size_t(k) * n + y] = w[size_t(y) * derivation + k];
+            }
+        }
+        m->fp_idx4.alloc(it4.size());
+        m->fp_w4.alloc(wt4.size());
+        h2d(m->fp_idx4.p, it4.data(), it4.size(), in->ctx);
+        h2d(m->fp_w4.p, wt4.data(), wt4.size(), in->ctx);
         *map = m.release();
     });
 }

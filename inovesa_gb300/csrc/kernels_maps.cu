@@ -230,19 +230,17 @@ __global__ void k_kick_y4(const float* __restrict__ in,
 // columns (their stencils, one per column, in registers for the block)
 // and sweeps the rows with 16-byte reads where the 4 columns take the
 // same shifts, column by column otherwise
-constexpr int KICKX_ROWS = 8;
-
 __global__ void k_kick_x4(const float* __restrict__ in,
                           float* __restrict__ out,
                           const float* __restrict__ offsets, uint32_t n,
-                          int it)
+                          int it, int rows)
 {
     const int n4 = int(n / 4);
     const size_t nxy = size_t(n) * n;
     const float* src = in + blockIdx.y * nxy;
     float* dst = out + blockIdx.y * nxy;
-    const int xa = blockIdx.x * KICKX_ROWS;
-    const int xe = min(int(n), xa + KICKX_ROWS);
+    const int xa = blockIdx.x * rows;
+    const int xe = min(int(n), xa + rows);
     for (int g = threadIdx.x; g < n4; g += blockDim.x) {
         KickStencil s[4];
 #pragma unroll
@@ -293,10 +291,11 @@ __global__ void k_kick_x4(const float* __restrict__ in,
 
 // Fokker-Planck: a CTA per block of rows of one bunch, the rows staged in
 // shared memory by 16-byte reads; each thread owns 4 columns, whose
-// stencils (ip <= 4 taps: column index and weight) it loads once
+// stencils (ip <= 4 taps: column index and weight, tap-major tables
+// [4][n]) it reads with 16-byte loads before the rows arrive
 __global__ void k_fp4(const float* __restrict__ in, float* __restrict__ out,
-                      const uint32_t* __restrict__ idx,
-                      const float* __restrict__ w, uint32_t n, int ip,
+                      const uint32_t* __restrict__ idx4,
+                      const float* __restrict__ w4, uint32_t n, int ip,
                       int rows)
 {
     extern __shared__ float4 blk4[];
@@ -305,6 +304,18 @@ __global__ void k_fp4(const float* __restrict__ in, float* __restrict__ out,
     const int xa = blockIdx.x * rows;
     const int nr = min(int(n) - xa, rows);
     const size_t base = (blockIdx.y * size_t(n) + xa) * n;
+    // this thread's first group's stencils (one group per thread when
+    // n <= 1024)
+    uint4 ixv[4];
+    float4 wtv[4];
+    const int g0 = threadIdx.x < n4 ? threadIdx.x : 0;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        ixv[j] = __ldg(reinterpret_cast<const uint4*>(idx4 + size_t(j) * n)
+                       + g0);
+        wtv[j] = __ldg(reinterpret_cast<const float4*>(w4 + size_t(j) * n)
+                       + g0);
+    }
     const float4* src = reinterpret_cast<const float4*>(in + base);
     for (int i = threadIdx.x; i < nr * n4; i += blockDim.x) {
         blk4[i] = __ldg(src + i);
@@ -312,16 +323,27 @@ __global__ void k_fp4(const float* __restrict__ in, float* __restrict__ out,
     __syncthreads();
     float4* dst = reinterpret_cast<float4*>(out + base);
     for (int g = threadIdx.x; g < n4; g += blockDim.x) {
+        if (g != g0) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                ixv[j] = __ldg(reinterpret_cast<const uint4*>(
+                                   idx4 + size_t(j) * n) + g);
+                wtv[j] = __ldg(reinterpret_cast<const float4*>(
+                                   w4 + size_t(j) * n) + g);
+            }
+        }
         uint32_t ix[4][4];
         float wt[4][4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const size_t k = size_t(4 * g + c) * ip + j;
-                ix[c][j] = j < ip ? idx[k] : 0u;
-                wt[c][j] = j < ip ? w[k] : 0.f;
-            }
+        for (int j = 0; j < 4; j++) {
+            ix[0][j] = ixv[j].x;
+            ix[1][j] = ixv[j].y;
+            ix[2][j] = ixv[j].z;
+            ix[3][j] = ixv[j].w;
+            wt[0][j] = wtv[j].x;
+            wt[1][j] = wtv[j].y;
+            wt[2][j] = wtv[j].z;
+            wt[3][j] = wtv[j].w;
         }
         for (int r = 0; r < nr; r++) {
             const float* rowp = blk + size_t(r) * n;
@@ -432,6 +454,14 @@ bool plain_v4(uint32_t n)
     return n % 4 == 0 && n <= PLAIN_V4_MAX;
 }
 
+// rows per CTA of k_kick_x4 and k_fp4: one, unless the meshes give more
+// than 4 CTAs per SM (152 SMs) with one; at most 8
+int plain_rows(uint32_t n, uint32_t nb)
+{
+    const size_t per = size_t(n) * nb / (4 * 152);
+    return int(std::max<size_t>(1, std::min<size_t>(8, per)));
+}
+
 void launch_kick(const vfps_map* m, const float* offset)
 {
     const vfps_ps* in = m->in;
@@ -443,9 +473,10 @@ void launch_kick(const vfps_map* m, const float* offset)
         k_kick_y4<<<in->nb * n, t4, smem, in->ctx->stream>>>(
             in->data.p, m->out->data.p, offset, n, m->it);
     } else if (v4) {
-        dim3 grid((n + KICKX_ROWS - 1) / KICKX_ROWS, in->nb);
+        const int rows = plain_rows(n, in->nb);
+        dim3 grid((n + rows - 1) / rows, in->nb);
         k_kick_x4<<<grid, t4, 0, in->ctx->stream>>>(
-            in->data.p, m->out->data.p, offset, n, m->it);
+            in->data.p, m->out->data.p, offset, n, m->it, rows);
     } else if (m->axis == VFPS_AXIS_Y) {
         const int threads = n >= 256 ? 256 : ((n + 31) / 32) * 32;
         k_kick_y<<<in->nb * n, threads, 0, in->ctx->stream>>>(
@@ -463,14 +494,15 @@ void launch_fp(const vfps_map* m)
     const vfps_ps* in = m->in;
     const uint32_t n = in->n;
     if (plain_v4(n) && m->ip <= 4 && !m->cells) {
-        // 8 rows of up to 1024 floats (32 KiB), fewer for wider meshes
-        const int rows = int(std::max<uint32_t>(1, std::min<uint32_t>(
-            8, 8192 / n)));
+        // at most 8 rows of up to 1024 floats (32 KiB), fewer for wider
+        // meshes
+        const int rows = std::min(plain_rows(n, in->nb),
+                                  int(std::max<uint32_t>(1, 8192 / n)));
         const int t4 = int(std::min<uint32_t>(256, ((n / 4 + 31) / 32) * 32));
         dim3 grid((n + rows - 1) / rows, in->nb);
         k_fp4<<<grid, t4, size_t(rows) * n * sizeof(float),
-                in->ctx->stream>>>(in->data.p, m->out->data.p, m->fp_idx.p,
-                                   m->fp_w.p, n, m->ip, rows);
+                in->ctx->stream>>>(in->data.p, m->out->data.p,
+                                   m->fp_idx4.p, m->fp_w4.p, n, m->ip, rows);
         VFPS_LAUNCHED();
         return;
     }

@@ -210,6 +210,8 @@ struct vfps_map {
     float e1 = 0;
     vfps::DevBuf<uint32_t> fp_idx;
     vfps::DevBuf<float> fp_w;
+    vfps::DevBuf<uint32_t> fp_idx4;        // the same, tap-major [4][n]
+    vfps::DevBuf<float> fp_w4;
     std::vector<uint32_t> h_fp_idx;
     std::vector<float> h_fp_w;
 };
