@@ -44,11 +44,14 @@ using vfps::DevBuf;
 // ================================================================== host
 enum {
     TL_RING = 0, TL_ROT = 1, TL_WIDE = 2, TL_RING4 = 3, TL_RINGF = 4,
-    TL_RINGF128 = 5, TL_RINGF64 = 6, TL_RINGF512 = 7, TL_COUNT = 8
+    TL_RINGF128 = 5, TL_RINGF64 = 6, TL_RINGF512 = 7, TL_RINGF1024 = 8,
+    TL_COUNT = 9
 };
 constexpr int RING_MAX_N = 256;   // widest mesh of the ring kernel, G = 2
 constexpr int RING4_N = 512;      // the mesh of the ring kernel, G = 4
 constexpr int RTHREADS4 = 256;    // its CTA: 8 warps, one row each
+constexpr int RINGF_WIDE_N = 1024;  // the widest mesh of the fast kernel
+constexpr int RTHREADSF1024 = 256;  // its CTA: two rows of 4 parts at once
 
 struct vfps_batch {
     vfps_ctx* ctx = nullptr;
@@ -56,11 +59,11 @@ struct vfps_batch {
     uint32_t nb = 0;
     std::vector<vfps_bunch_desc> desc;
     std::vector<BDev> hb;
-    // tile lists: TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512 (chain
-    // 0, n = 256, 128, 64, 512, regular lattices: the fast ring kernel),
-    // TL_RING (the other chain-0 meshes up to 256 rows), TL_RING4 (the
-    // other chain-0 meshes of 512 rows), TL_ROT (chain 1), TL_WIDE (chain
-    // 0, n = 1024)
+    // tile lists: TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512,
+    // TL_RINGF1024 (chain 0, n = 256, 128, 64, 512, 1024, regular
+    // lattices: the fast ring kernel), TL_RING (the other chain-0 meshes up
+    // to 256 rows), TL_RING4 (the other chain-0 meshes of 512 rows), TL_ROT
+    // (chain 1), TL_WIDE (the other chain-0 meshes of 1024 rows)
     std::vector<Tile> htiles[TL_COUNT];
     size_t cells = 0, rows = 0;
     uint32_t max_n = 0;
@@ -88,8 +91,8 @@ struct vfps_batch {
     unsigned gridR = 0;        // persistent CTAs of k_bmaps0
     SmemR layoutR4{};          // the same for the 512-row ring kernel
     unsigned gridR4 = 0;
-    SmemR layoutRF[4] = {};    // the same for the fast ring kernel, per
-    unsigned gridRF[4] = {};   // mesh size 256, 128, 64, 512
+    SmemR layoutRF[5] = {};    // the same for the fast ring kernel, per
+    unsigned gridRF[5] = {};   // mesh size 256, 128, 64, 512, 1024
     unsigned grid0 = 0;        // persistent CTAs of k_bmaps0w
     int tile_cells = 0;
     int tile_rows = 0;
@@ -234,8 +237,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     // that each fills the SMs the others leave free (no kernel's tail
     // idles the GPU); sequential when the kernels are timed one by one
     int classes = 0;
-    for (int c : {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512, TL_RING,
-                  TL_RING4, TL_WIDE, TL_ROT}) {
+    for (int c : {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512,
+                  TL_RINGF1024, TL_RING, TL_RING4, TL_WIDE, TL_ROT}) {
         classes += b->htiles[c].empty() ? 0 : 1;
     }
     const bool forked = !ev && classes > 1;
@@ -279,6 +282,8 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
                 b->layoutRF[2], (const RowInfo7*)b->rinfo7.p);
     ring_launch(k_bmaps0f<RTHREADS, 512>, TL_RINGF512, b->gridRF[3],
                 RTHREADS, b->layoutRF[3], (const RowInfo7*)b->rinfo7.p);
+    ring_launch(k_bmaps0f<RTHREADSF1024, 1024>, TL_RINGF1024, b->gridRF[4],
+                RTHREADSF1024, b->layoutRF[4], (const RowInfo7*)b->rinfo7.p);
     ring_launch(k_bmaps0<2, RTHREADS>, TL_RING, b->gridR, RTHREADS,
                 b->layoutR, (const RowInfo*)b->rinfo.p);
     ring_launch(k_bmaps0<4, RTHREADS4>, TL_RING4, b->gridR4, RTHREADS4,
@@ -337,7 +342,7 @@ void build_tiles(vfps_batch* b, int tile_cells)
     // regions sized for the largest tile of each kernel
     size_t a_floats = 0, b_floats = 0, t_floats = 0, s_rows = 0, p_rows = 0;
     int ring_rows = 0, ring_n = 0, ring4_rows = 0;
-    int ringf_rows[4] = {0, 0, 0, 0};
+    int ringf_rows[5] = {0, 0, 0, 0, 0};
     for (uint32_t i = 0; i < b->nb; i++) {
         const BDev& B = b->hb[i];
         const int n = int(B.n);
@@ -351,11 +356,14 @@ void build_tiles(vfps_batch* b, int tile_cells)
                              : (n == RING4_N ? ((B.flags & F_Y7)
                                                     ? TL_RINGF512
                                                     : TL_RING4)
-                                             : TL_WIDE));
+                                             : ((B.flags & F_Y7)
+                                                    ? TL_RINGF1024
+                                                    : TL_WIDE)));
         const int fk = c == TL_RINGF ? 0
                        : c == TL_RINGF128 ? 1
                        : c == TL_RINGF64 ? 2
-                       : c == TL_RINGF512 ? 3 : -1;
+                       : c == TL_RINGF512 ? 3
+                       : c == TL_RINGF1024 ? 4 : -1;
         int tx = std::max(4, tile_cells / n);
         if (c == TL_RING || c == TL_RING4 || fk >= 0) {
             // the ring holds two tiles with their halos: at most 32 staged
@@ -393,29 +401,34 @@ void build_tiles(vfps_batch* b, int tile_cells)
         o = align16(o + bytes);
     };
     // the ring holds the staged rows of two tiles with their halos
+    // parts: the fast kernel's row parts on 512- and 1024-row meshes
+    // (their sums of two tiles), planes: the drift and Fokker-Planck table
     auto ring_layout = [&](SmemR& L, int rows, int n, size_t rec,
-                           bool halves = false) {
+                           int parts = 0, int planes = 10) {
         const int rb = 2 * rows;
         L.rb = static_cast<uint32_t>(rb);
         L.rs = static_cast<uint32_t>(astride0(n));
         o = 0;
         take(&L.ring, size_t(rb) * L.rs * 4);
         take(&L.s, size_t(rows) * rec);
-        take(&L.tab, size_t(10) * n * 4);
-        take(&L.part, halves ? size_t(2) * rb * 4 : 0);
+        take(&L.tab, size_t(planes) * n * 4);
+        take(&L.part, size_t(parts) * rb * 4);
         take(&L.bar, 3 * sizeof(uint64_t));
         L.total = static_cast<uint32_t>(o);
         return o;
     };
-    const int flist[4] = {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512};
-    const int fn[4] = {256, 128, 64, 512};
-    for (int k = 0; k < 4; k++) {
+    const int flist[5] = {TL_RINGF, TL_RINGF128, TL_RINGF64, TL_RINGF512,
+                          TL_RINGF1024};
+    const int fn[5] = {256, 128, 64, 512, 1024};
+    for (int k = 0; k < 5; k++) {
         const int c = flist[k];
         if (b->htiles[c].empty()) {
             continue;
         }
         b->smem[c] = ring_layout(b->layoutRF[k], ringf_rows[k], fn[k],
-                                 sizeof(RowInfo7), fn[k] > RING_MAX_N);
+                                 sizeof(RowInfo7),
+                                 fn[k] > RING_MAX_N ? fn[k] / 256 : 0,
+                                 fn[k] == RINGF_WIDE_N ? 11 : 10);
         const size_t nt = b->htiles[c].size();
         b->gridRF[k] =
             k == 0 ? persistent_grid(b, k_bmaps0f<RTHREADS, 256>, RTHREADS,
@@ -424,8 +437,10 @@ void build_tiles(vfps_batch* b, int tile_cells)
                                        b->smem[c], nt)
             : k == 2 ? persistent_grid(b, k_bmaps0f<RTHREADS, 64>, RTHREADS,
                                        b->smem[c], nt)
-                     : persistent_grid(b, k_bmaps0f<RTHREADS, 512>, RTHREADS,
-                                       b->smem[c], nt);
+            : k == 3 ? persistent_grid(b, k_bmaps0f<RTHREADS, 512>, RTHREADS,
+                                       b->smem[c], nt)
+                     : persistent_grid(b, k_bmaps0f<RTHREADSF1024, 1024>,
+                                       RTHREADSF1024, b->smem[c], nt);
     }
     if (!b->htiles[TL_RING].empty()) {
         b->smem[TL_RING] = ring_layout(b->layoutR, ring_rows, ring_n,
@@ -492,6 +507,10 @@ void upload_tiles(vfps_batch* b)
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
                                        b->smem[TL_RINGF512], 1))));
+    VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0f<RTHREADSF1024, 1024>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(std::max<size_t>(
+                                       b->smem[TL_RINGF1024], 1))));
     VFPS_CUDA(cudaFuncSetAttribute(k_bmaps0<2, RTHREADS>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(std::max<size_t>(
@@ -770,21 +789,25 @@ std::vector<float> fp_weights(const vfps::Axis& ay, float e1, int fptype,
     return w5;
 }
 
-// The lattice forms k_bmaps0f takes: every aligned group of 4 energy
-// columns has one drift shift (its lanes load one window row per group),
-// and the Fokker-Planck stencils of the lower half of the energy columns
+// The lattice forms k_bmaps0f takes: the drift shifts of every aligned
+// group of 4 energy columns differ by at most `spread` (0: one window of 4
+// rows per group; 1: the 5-row window of 1024-row meshes), and the
+// Fokker-Planck stencils of the lower half of the energy columns
 // reach offsets -2..1 only, those of the upper half -1..2 only (4 taps),
 // except the last column of the lower half, which may reach -2..2 (the
 // reference starts its upper stencils at the truncated centre, which is
 // that column on a mesh centred on the reference energy)
 bool fast_ring_ok(const std::vector<RowStencil>& dr,
-                  const std::vector<float>& w5, uint32_t n)
+                  const std::vector<float>& w5, uint32_t n, int spread)
 {
     for (uint32_t y = 0; y < n; y += 4) {
+        int lo = dr[y].shift0, hi = dr[y].shift0;
         for (uint32_t c = 1; c < 4; c++) {
-            if (dr[y + c].shift0 != dr[y].shift0) {
-                return false;
-            }
+            lo = std::min(lo, dr[y + c].shift0);
+            hi = std::max(hi, dr[y + c].shift0);
+        }
+        if (hi - lo > spread) {
+            return false;
         }
     }
     for (uint32_t y = 0; y < n; y++) {
@@ -964,22 +987,6 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             sts.insert(sts.end(), dr.begin(), dr.end());
             pws.push_back(pwd);
             if (d.chain == 0) {
-                // drift stencils as planes for 16-byte loads: w[j][y] for
-                // j < 4, then shift0[y] (int bits), then the Fokker-Planck
-                // weights as planes F[o][y] for the offsets -2..2 (the
-                // identity without Fokker-Planck)
-                std::vector<float> tab;
-                tab.reserve(size_t(n) * 10);
-                for (int j = 0; j < 4; j++) {
-                    for (uint32_t y = 0; y < n; y++) {
-                        tab.push_back(dr[y].w[j]);
-                    }
-                }
-                for (uint32_t y = 0; y < n; y++) {
-                    float f;
-                    std::memcpy(&f, &dr[y].shift0, sizeof(f));
-                    tab.push_back(f);
-                }
                 std::vector<float> w5(size_t(n) * 5, 0.f);
                 if (d.e1 > 0) {
                     w5 = fp_weights(ay, float(d.e1), d.fptype, d.derivation);
@@ -988,15 +995,56 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                         w5[size_t(y) * 5 + 2] = 1.f;
                     }
                 }
+                // 1024 rows: the fast kernel's 5-row window (a group of 4
+                // columns may span two drift shifts)
+                const bool win5 = n == RINGF_WIDE_N;
+                if ((n <= RING_MAX_N || n == RING4_N || win5)
+                    && fast_ring_ok(dr, w5, n, win5 ? 1 : 0)
+                    && !fast_ring_off()) {
+                    B.flags |= F_Y7;
+                }
+                // drift stencils as planes for 16-byte loads: w[j][y] for
+                // j < 4, then shift0[y] (int bits), then the Fokker-Planck
+                // weights as planes F[o][y] for the offsets -2..2 (the
+                // identity without Fokker-Planck).  The 5-row window's
+                // table: planes j < 5 of the taps from the group's lowest
+                // shift (a column one shift higher has a zero in plane 0,
+                // the others a zero in plane 4), the group's lowest shift
+                // for every column
+                std::vector<float> tab;
+                const bool t5 = win5 && (B.flags & F_Y7);
+                tab.reserve(size_t(n) * (t5 ? 11 : 10));
+                std::vector<int> gshift(n);
+                for (uint32_t y = 0; y < n; y++) {
+                    gshift[y] = dr[y].shift0;
+                    if (t5) {
+                        const uint32_t g = y & ~3u;
+                        gshift[y] = std::min(std::min(dr[g].shift0,
+                                                      dr[g + 1].shift0),
+                                             std::min(dr[g + 2].shift0,
+                                                      dr[g + 3].shift0));
+                    }
+                }
+                for (int j = 0; j < (t5 ? 5 : 4); j++) {
+                    for (uint32_t y = 0; y < n; y++) {
+                        const int k = j - (dr[y].shift0 - gshift[y]);
+                        tab.push_back(k >= 0 && k < 4 ? dr[y].w[k] : 0.f);
+                    }
+                }
+                for (uint32_t y = 0; y < n; y++) {
+                    float f;
+                    std::memcpy(&f, &gshift[y], sizeof(f));
+                    tab.push_back(f);
+                }
                 for (int o = 0; o < 5; o++) {
                     for (uint32_t y = 0; y < n; y++) {
                         tab.push_back(w5[size_t(y) * 5 + o]);
                     }
                 }
-                if ((n <= RING_MAX_N || n == RING4_N)
-                    && fast_ring_ok(dr, w5, n)
-                    && !fast_ring_off()) {
-                    B.flags |= F_Y7;
+                if (t5) {
+                    // the fifth row of a window lies one past the rows the
+                    // stencils read: one more staged row below the tile
+                    B.halo_hi += 1;
                 }
                 // bunches of a scan share these tables: one copy each, so
                 // that a ring kernel's CTA stages a shared one only once
@@ -1555,7 +1603,8 @@ extern "C" int vfps_batch_kernel_tiles(const vfps_batch* b, uint32_t* tiles,
     if (count > 0) {   // the fast ring kernel: every mesh size
         tiles[0] += static_cast<uint32_t>(b->htiles[TL_RINGF128].size()
                                           + b->htiles[TL_RINGF64].size()
-                                          + b->htiles[TL_RINGF512].size());
+                                          + b->htiles[TL_RINGF512].size()
+                                          + b->htiles[TL_RINGF1024].size());
     }
     return VFPS_OK;
 }

@@ -156,16 +156,32 @@ __device__ __forceinline__ float4 fp4(const float (&w)[7], const float4& f0,
     return make_float4(o[0], o[1], o[2], o[3]);
 }
 
-// N: the mesh size of every bunch of the tile list (64, 128, 256 or 512;
-// the lane mapping, strides and shuffle widths are constants)
+// meshes of 512 and 1024 rows: rows in parts of 256 columns, one warp each
+// in stage 2; 1024-row lattices take a 5-row drift window (groups of 4
+// columns may span two drift shifts) and an 11-plane table
+template <int N>
+struct RingShape {
+    static constexpr bool HALF = N > 256;
+    static constexpr int PARTS = HALF ? N / 256 : 1;
+    static constexpr int WIN = N >= 1024 ? 5 : 4;
+    // drift planes, the shift, 5 Fokker-Planck planes
+    static constexpr int TAB_PLANES = WIN + 1 + 5;
+};
+
+// N: the mesh size of every bunch of the tile list (64, 128, 256, 512 or
+// 1024; the lane mapping, strides and shuffle widths are constants)
 template <int NT, int N>
-__global__ void __launch_bounds__(NT, N > 256 ? 2 : 3)
+__global__ void __launch_bounds__(NT, N >= 1024 ? 1 : (N > 256 ? 2 : 3))
 k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
           uint32_t ntiles, const float* __restrict__ tabs,
           const float* __restrict__ dwt, const RowInfo7* __restrict__ rinfo,
           const float* __restrict__ din, float* __restrict__ dout,
           float* __restrict__ pout, int* __restrict__ status, SmemR L)
 {
+    constexpr bool HALF = RingShape<N>::HALF;
+    constexpr int PARTS = RingShape<N>::PARTS;
+    constexpr int WIN = RingShape<N>::WIN;
+    constexpr int TAB_PLANES = RingShape<N>::TAB_PLANES;
     extern __shared__ float4 smem4[];
     char* base = reinterpret_cast<char*>(smem4);
     float* ring = reinterpret_cast<float*>(base + L.ring);
@@ -209,7 +225,7 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     uint32_t tab_off = 0xffffffffu, tab_ph = 0;
     bool tab_wait = false;
     auto load_tab = [&](const BDev& Bt) {
-        const uint32_t bytes = 10u * Bt.n * 4u;
+        const uint32_t bytes = uint32_t(TAB_PLANES) * Bt.n * 4u;
         if (threadIdx.x == 0) {
             fence_proxy_async();
             mbar_arrive_expect_tx(&bar[2], bytes);
@@ -240,14 +256,19 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                    false, true);
     }
     int bad = 0;
-    constexpr bool HALF = N > 256;
-    // the previous tile's row sums (512 rows): stored after a barrier
+    // the previous tile's row sums (512 and 1024 rows: one part per warp of
+    // a row, added in part order and stored after a barrier)
     int prev_off = 0, prev_rows = 0;
     float prev_h03 = 0.f;
     auto store_halves = [&](int buf) {
-        const float* p0 = part + buf * rb;
+        const float* p0 = part + buf * PARTS * (rb >> 1);
         for (int i = threadIdx.x; i < prev_rows; i += NT) {
-            pout[prev_off + i] = prev_h03 * (p0[i] + p0[i + (rb >> 1)]);
+            float v = p0[i];
+#pragma unroll
+            for (int q = 1; q < PARTS; q++) {
+                v += p0[i + q * (rb >> 1)];
+            }
+            pout[prev_off + i] = prev_h03 * v;
         }
     };
     for (uint32_t k = 0, tid = t_begin; tid < t_end; tid++, k++) {
@@ -256,7 +277,7 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
         constexpr int n = N;
         const int x0 = int(t.x0);
         const int rows = int(t.rows);
-        constexpr int G1 = HALF ? 4 : 2;     // column groups per lane
+        constexpr int G1 = HALF ? N / 128 : 2;   // column groups per lane
         constexpr int seg = N / (4 * G1);    // lanes per row (stage 1)
         const int l = threadIdx.x & (seg - 1);
         const int rl = threadIdx.x / seg;    // segment
@@ -523,23 +544,33 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 flush(X, p0, p1, p2, p3);
             }
         } else {
-            // a pair of warps per run of output rows: warp h of the pair
-            // takes columns [h n/2, (h + 1) n/2), its lane l the groups at
-            // h n/2 + 4l (A) and h n/2 + n/4 + 4l (B); both groups of the
+            // PARTS warps per run of output rows: warp h of a group takes
+            // the part of columns [256h, 256h + 256), its lane l the groups
+            // at 256h + 4l (A) and 256h + 128 + 4l (B); the parts of the
             // lower half take the stencil's lower form (offsets -2..1,
             // planes 0..3), those of the upper half the upper form (-1..2,
-            // planes 1..4).  The columns past the half that the stencils
-            // reach (n/2, n/2 + 1 below; n/2 - 1 above) come from a third,
-            // 2-column window (C) of the same rows
-            const float* W = T;
-            const float* F = T + 5 * n;
+            // planes 1..4).  The columns just left and right of its part
+            // that a warp's stencils reach come from two 2-column windows
+            // of the same staged rows, C (256h - 2, 256h - 1) and D
+            // (256h + 256, 256h + 257), with the same drift arithmetic as
+            // their own warps', so no value crosses between warps (at the
+            // mesh edges C and D repeat columns 0, 1 or n - 2, n - 1, which
+            // meet the zero stencils of those columns).  With two parts
+            // each has one inner edge: one window, the edge lanes' mesh
+            // edge neighbours wrapped around the warp.  WIN staged rows
+            // per window: 4, or 5 where a group of 4 columns spans two
+            // drift shifts (its table holds 5 planes from the group's
+            // lowest shift, with a zero where a column's stencil ends)
+            const float* W = T;                     // drift [WIN][n], shift
+            const float* F = T + (WIN + 1) * n;     // Fokker-Planck [5][n]
             const float h03 = tabs[B.tab_off + TAB_WS * n];
-            const int h = rl & 1;
-            constexpr int pairs = rp >> 1;
-            const int per = (rows + pairs - 1) / pairs;
-            const int ra = (rl >> 1) * per;
+            const int h = rl % PARTS;
+            constexpr int groups = rp / PARTS;
+            const int per = (rows + groups - 1) / groups;
+            const int ra = (rl / PARTS) * per;
             const int xend = x0 + min(rows, ra + per);
-            float* psum = part + (k & 1) * rb + h * (rb >> 1) - x0;
+            float* psum = part + (k & 1) * PARTS * (rb >> 1)
+                          + h * (rb >> 1) - x0;
             auto slot0 = [&](int x) {
                 int q = (x + mc.off) % rb;
                 return q < 0 ? q + rb : q;
@@ -548,25 +579,33 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 o += rs;
                 o -= o >= ring_floats ? ring_floats : 0;
             };
-            const bool first = l == 0, last = l == 31;
+            const bool first = h == 0 && l == 0;
+            const bool last = h == PARTS - 1 && l == 31;
+            const bool lfirst = l == 0, llast = l == 31;
             const int lm = (l + 31) & 31, lp = (l + 1) & 31;
             float* obase = dout + B.dens_off;
-            auto walk = [&](auto hc) {
-                constexpr int H = decltype(hc)::value;
-                constexpr int P0 = H;           // first Fokker-Planck plane
-                const int yA = H * (n >> 1) + 4 * l;
-                const int yB = yA + (n >> 2);
-                constexpr int yC = H == 0 ? (n >> 1) : (n >> 1) - 2;
-                const int shA = __float_as_int(W[4 * n + yA]);
-                const int shB = __float_as_int(W[4 * n + yB]);
-                const int shC = __float_as_int(W[4 * n + yC]);
-                float4 wA[4], wB[4];
-                float2 wC[4];
+            constexpr bool TWO = PARTS == 2;
+            auto walk = [&](auto lc) {
+                constexpr bool LOWER = decltype(lc)::value != 0;
+                constexpr int P0 = LOWER ? 0 : 1;   // first Fokker-Planck plane
+                const int yA = 256 * h + 4 * l;
+                const int yB = yA + 128;
+                const int yC = TWO ? (LOWER ? 256 * h + 256 : 256 * h - 2)
+                                   : (h == 0 ? 0 : 256 * h - 2);
+                const int yD = TWO ? yC
+                                   : (h == PARTS - 1 ? n - 2 : 256 * h + 256);
+                const int shA = __float_as_int(W[WIN * n + yA]);
+                const int shB = __float_as_int(W[WIN * n + yB]);
+                const int shC = __float_as_int(W[WIN * n + yC]);
+                const int shD = __float_as_int(W[WIN * n + yD]);
+                float4 wA[WIN], wB[WIN];
+                float2 wC[WIN], wD[WIN];
 #pragma unroll
-                for (int j = 0; j < 4; j++) {
+                for (int j = 0; j < WIN; j++) {
                     wA[j] = *reinterpret_cast<const float4*>(W + j * n + yA);
                     wB[j] = *reinterpret_cast<const float4*>(W + j * n + yB);
                     wC[j] = *reinterpret_cast<const float2*>(W + j * n + yC);
+                    wD[j] = *reinterpret_cast<const float2*>(W + j * n + yD);
                 }
                 auto fw = [&](int o, int y) {
                     return *reinterpret_cast<const float4*>(F + o * n + y);
@@ -574,85 +613,125 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 int oA = slot0(x0 + ra + shA) * rs + APAD + yA;
                 int oB = slot0(x0 + ra + shB) * rs + APAD + yB;
                 int oC = slot0(x0 + ra + shC) * rs + APAD + yC;
-                float4 a0, a1, a2, a3, b0, b1, b2, b3;
-                float2 c0, c1, c2, c3;
-                a0 = *reinterpret_cast<const float4*>(ring + oA);
-                b0 = *reinterpret_cast<const float4*>(ring + oB);
-                c0 = *reinterpret_cast<const float2*>(ring + oC);
-                next(oA);
-                next(oB);
-                next(oC);
-                a1 = *reinterpret_cast<const float4*>(ring + oA);
-                b1 = *reinterpret_cast<const float4*>(ring + oB);
-                c1 = *reinterpret_cast<const float2*>(ring + oC);
-                next(oA);
-                next(oB);
-                next(oC);
-                a2 = *reinterpret_cast<const float4*>(ring + oA);
-                b2 = *reinterpret_cast<const float4*>(ring + oB);
-                c2 = *reinterpret_cast<const float2*>(ring + oC);
-                next(oA);
-                next(oB);
-                next(oC);
-                // offset +2 of the lower half: zero but in its last column
-                // n/2 - 1 (the last lane's 4th of B), whose neighbour
-                // n/2 + 1 is C's second column
-                const float f4b = H == 0 ? F[4 * n + yB + 3] : 0.f;
-                auto one = [&](int X, const float4& r0, const float4& r1,
-                               const float4& r2, float4& r3, const float4& s0,
-                               const float4& s1, const float4& s2, float4& s3,
-                               const float2& t0, const float2& t1,
-                               const float2& t2, float2& t3) {
-                    r3 = *reinterpret_cast<const float4*>(ring + oA);
-                    s3 = *reinterpret_cast<const float4*>(ring + oB);
-                    t3 = *reinterpret_cast<const float2*>(ring + oC);
+                int oD = slot0(x0 + ra + shD) * rs + APAD + yD;
+                // the windows: slots 0..WIN-2 loaded here, the newest row
+                // by one()
+                float4 a[WIN], bw[WIN];
+                float2 c[WIN];
+                [[maybe_unused]] float2 dd[WIN];   // not with two parts
+                auto load = [&](int j) {
+                    a[j] = *reinterpret_cast<const float4*>(ring + oA);
+                    bw[j] = *reinterpret_cast<const float4*>(ring + oB);
+                    c[j] = *reinterpret_cast<const float2*>(ring + oC);
                     next(oA);
                     next(oB);
                     next(oC);
-                    const float4 dA = drift4(r0, r1, r2, r3, wA);
-                    const float4 dB = drift4(s0, s1, s2, s3, wB);
-                    const float2 dC = drift2(t0, t1, t2, t3, wC);
+                    if constexpr (!TWO) {
+                        dd[j] = *reinterpret_cast<const float2*>(ring + oD);
+                        next(oD);
+                    }
+                };
+#pragma unroll
+                for (int j = 0; j < WIN - 1; j++) {
+                    load(j);
+                }
+                // offset +2 of the lower half: zero but in its last column
+                // n/2 - 1 (the last lane's 4th of B in the last lower
+                // part), whose neighbour n/2 + 1 is D's second column
+                const float f4b = LOWER ? F[4 * n + yB + 3] : 0.f;
+                // output row X from window slots S0 .. S0 + WIN - 1 (mod
+                // WIN), the newest of them loaded here
+                auto one = [&](int X, auto sc) -> float {
+                    constexpr int S0 = decltype(sc)::value;
+                    constexpr int S1 = (S0 + 1) % WIN, S2 = (S0 + 2) % WIN,
+                                  S3 = (S0 + 3) % WIN;
+                    constexpr int SN = (S0 + WIN - 1) % WIN;
+                    load(SN);
+                    const float4 wa4[4] = {wA[0], wA[1], wA[2], wA[3]};
+                    const float4 wb4[4] = {wB[0], wB[1], wB[2], wB[3]};
+                    const float2 wc2[4] = {wC[0], wC[1], wC[2], wC[3]};
+                    const float2 wd2[4] = {wD[0], wD[1], wD[2], wD[3]};
+                    float4 dA = drift4(a[S0], a[S1], a[S2], a[S3], wa4);
+                    float4 dB = drift4(bw[S0], bw[S1], bw[S2], bw[S3], wb4);
+                    float2 dC = drift2(c[S0], c[S1], c[S2], c[S3], wc2);
+                    float2 dD = dC;
+                    if constexpr (!TWO) {
+                        dD = drift2(dd[S0], dd[S1], dd[S2], dd[S3], wd2);
+                    }
+                    if constexpr (WIN == 5) {
+                        // the fifth tap: one more packed FMA per pair (a
+                        // zero weight where a column's stencil ends at the
+                        // fourth, which keeps its sum's bits)
+                        const float4 r4 = a[SN], s4 = bw[SN];
+                        float2 lo = __ffma2_rn(make_float2(wA[4].x, wA[4].y),
+                                               make_float2(r4.x, r4.y),
+                                               make_float2(dA.x, dA.y));
+                        float2 hi = __ffma2_rn(make_float2(wA[4].z, wA[4].w),
+                                               make_float2(r4.z, r4.w),
+                                               make_float2(dA.z, dA.w));
+                        dA = make_float4(lo.x, lo.y, hi.x, hi.y);
+                        lo = __ffma2_rn(make_float2(wB[4].x, wB[4].y),
+                                        make_float2(s4.x, s4.y),
+                                        make_float2(dB.x, dB.y));
+                        hi = __ffma2_rn(make_float2(wB[4].z, wB[4].w),
+                                        make_float2(s4.z, s4.w),
+                                        make_float2(dB.z, dB.w));
+                        dB = make_float4(lo.x, lo.y, hi.x, hi.y);
+                        dC = __ffma2_rn(wC[4], c[SN], dC);
+                        if constexpr (!TWO) {
+                            dD = __ffma2_rn(wD[4], dd[SN], dD);
+                        } else {
+                            dD = dC;
+                        }
+                    }
                     float4 fA, fB;
-                    if constexpr (H == 0) {
-                        // A: left lane l-1's A2, A3 (lane 0: lane 31's,
-                        // meeting the zero stencils of columns 0, 1), right
-                        // lane l+1's A0 (lane 31: lane 0's B0); B: left
-                        // lane l-1's B2, B3 (lane 0: lane 31's A2, A3),
-                        // right lane l+1's B0 (lane 31: C's first column)
+                    if constexpr (LOWER) {
+                        // A: left lane l-1's A2, A3 (lane 0: C), right lane
+                        // l+1's A0 (lane 31: lane 0's B0); B: left lane
+                        // l-1's B2, B3 (lane 0: lane 31's A2, A3), right
+                        // lane l+1's B0 (lane 31: D's first column)
                         const float aL2 = __shfl_sync(0xffffffffu, dA.z, lm);
                         const float aL3 = __shfl_sync(0xffffffffu, dA.w, lm);
                         const float aR0 = __shfl_sync(0xffffffffu, dA.x, lp);
                         const float bL2 = __shfl_sync(0xffffffffu, dB.z, lm);
                         const float bL3 = __shfl_sync(0xffffffffu, dB.w, lm);
                         const float bR0 = __shfl_sync(0xffffffffu, dB.x, lp);
-                        const float wa[7] = {aL2, aL3, dA.x, dA.y, dA.z, dA.w,
-                                             last ? bR0 : aR0};
-                        const float wb[7] = {first ? aL2 : bL2,
-                                             first ? aL3 : bL3, dB.x, dB.y,
-                                             dB.z, dB.w, last ? dC.x : bR0};
+                        // (two parts: lane 0's left neighbours are lane
+                        // 31's A2, A3, meeting the zero stencils of
+                        // columns 0, 1)
+                        const float wa[7] = {(lfirst && !TWO) ? dC.x : aL2,
+                                             (lfirst && !TWO) ? dC.y : aL3,
+                                             dA.x, dA.y, dA.z, dA.w,
+                                             llast ? bR0 : aR0};
+                        const float wb[7] = {lfirst ? aL2 : bL2,
+                                             lfirst ? aL3 : bL3, dB.x, dB.y,
+                                             dB.z, dB.w, llast ? dD.x : bR0};
                         fA = fp4(wa, fw(P0, yA), fw(P0 + 1, yA),
                                  fw(P0 + 2, yA), fw(P0 + 3, yA));
                         fB = fp4(wb, fw(P0, yB), fw(P0 + 1, yB),
                                  fw(P0 + 2, yB), fw(P0 + 3, yB));
-                        fB.w = fmaf(f4b, dC.y, fB.w);
+                        fB.w = fmaf(f4b, dD.y, fB.w);
                     } else {
                         // A: left lane l-1's A3 (lane 0: C's second
                         // column), right lane l+1's A0, A1 (lane 31: lane
                         // 0's B0, B1); B: left lane l-1's B3 (lane 0: lane
-                        // 31's A3), right lane l+1's B0, B1 (lane 31: lane
-                        // 0's, meeting the zero stencils of columns n-2,
-                        // n-1)
+                        // 31's A3), right lane l+1's B0, B1 (lane 31: D)
                         const float aL3 = __shfl_sync(0xffffffffu, dA.w, lm);
                         const float aR0 = __shfl_sync(0xffffffffu, dA.x, lp);
                         const float aR1 = __shfl_sync(0xffffffffu, dA.y, lp);
                         const float bL3 = __shfl_sync(0xffffffffu, dB.w, lm);
                         const float bR0 = __shfl_sync(0xffffffffu, dB.x, lp);
                         const float bR1 = __shfl_sync(0xffffffffu, dB.y, lp);
-                        const float wa[7] = {first ? dC.y : aL3, dA.x, dA.y,
-                                             dA.z, dA.w, last ? bR0 : aR0,
-                                             last ? bR1 : aR1};
-                        const float wb[7] = {first ? aL3 : bL3, dB.x, dB.y,
-                                             dB.z, dB.w, bR0, bR1};
+                        const float wa[7] = {lfirst ? dC.y : aL3, dA.x, dA.y,
+                                             dA.z, dA.w, llast ? bR0 : aR0,
+                                             llast ? bR1 : aR1};
+                        // (two parts: lane 31's right neighbours are lane
+                        // 0's B0, B1, meeting the zero stencils of columns
+                        // n - 2, n - 1)
+                        const float wb[7] = {lfirst ? aL3 : bL3, dB.x, dB.y,
+                                             dB.z, dB.w,
+                                             (llast && !TWO) ? dD.x : bR0,
+                                             (llast && !TWO) ? dD.y : bR1};
                         fA = fp4(wa, fw(P0, yA), fw(P0 + 1, yA),
                                  fw(P0 + 2, yA), fw(P0 + 3, yA));
                         fB = fp4(wb, fw(P0, yB), fw(P0 + 1, yB),
@@ -667,15 +746,15 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                     // and n - 1 one
                     float e = (fA.x + fA.z) + (fB.x + fB.z);
                     float od = (fA.y + fA.w) + (fB.y + fB.w);
-                    if (H == 0 && first) {
+                    if (first) {
                         e -= 0.5f * fA.x;
                     }
-                    if (H == 1 && last) {
+                    if (last) {
                         od -= 0.75f * fB.w;
                     }
                     return fmaf(4.f, od, 2.f * e);
                 };
-                // the half's sums of 4 output rows: reduce-scatter over
+                // the part's sums of 4 output rows: reduce-scatter over
                 // the warp, one lane stores a row's
                 auto flush = [&](int X, float p0, float p1, float p2,
                                  float p3) {
@@ -696,21 +775,39 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                     }
                 };
                 for (int X = x0 + ra; X < x0 + ra + per; X += 4) {
-                    const float p0 = one(X, a0, a1, a2, a3, b0, b1, b2, b3,
-                                         c0, c1, c2, c3);
-                    const float p1 = one(X + 1, a1, a2, a3, a0, b1, b2, b3,
-                                         b0, c1, c2, c3, c0);
-                    const float p2 = one(X + 2, a2, a3, a0, a1, b2, b3, b0,
-                                         b1, c2, c3, c0, c1);
-                    const float p3 = one(X + 3, a3, a0, a1, a2, b3, b0, b1,
-                                         b2, c3, c0, c1, c2);
+                    const float p0 = one(X, IntC<0>{});
+                    const float p1 = one(X + 1, IntC<1>{});
+                    const float p2 = one(X + 2, IntC<2>{});
+                    const float p3 = one(X + 3, IntC<3>{});
                     flush(X, p0, p1, p2, p3);
+                    if constexpr (WIN == 5) {
+                        // 5 slots, 4 rows per step: slots 4, 0, 1, 2 hold
+                        // the next step's first 4 rows; move them to 0..3
+                        a[3] = a[2];
+                        a[2] = a[1];
+                        a[1] = a[0];
+                        a[0] = a[4];
+                        bw[3] = bw[2];
+                        bw[2] = bw[1];
+                        bw[1] = bw[0];
+                        bw[0] = bw[4];
+                        c[3] = c[2];
+                        c[2] = c[1];
+                        c[1] = c[0];
+                        c[0] = c[4];
+                        if constexpr (!TWO) {
+                            dd[3] = dd[2];
+                            dd[2] = dd[1];
+                            dd[1] = dd[0];
+                            dd[0] = dd[4];
+                        }
+                    }
                 }
             };
-            if (h == 0) {
-                walk(IntC<0>{});
-            } else {
+            if (h < PARTS / 2) {
                 walk(IntC<1>{});
+            } else {
+                walk(IntC<0>{});
             }
             prev_off = int(B.prof_off) + x0;
             prev_rows = rows;

@@ -5,6 +5,7 @@ FP64, checked after tens to hundreds of steps; profiles and wakes within
 the same bound.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -411,5 +412,55 @@ def test_fast_ring_kernel_512(gpu_ctx, monkeypatch):
         assert np.abs(prof - sums).max() <= 1e-5 * sums.max(), i
         ref = oracle_sim(p, ch, ib, z.data(), it=it, clamp=cl)
         ref.step(steps)
+        assert rel_l1(ga, ref.density(0)) <= TOL, i
+        assert rel_l1(fast.profile(i), ref.profile(0)) <= TOL, i
+
+
+def test_fast_ring_kernel_1024(gpu_ctx, monkeypatch):
+    """1024-row meshes on the lattice of the uneven workload (2000 steps per
+    period: drift offsets up to 1.6 cells, so some groups of 4 energy
+    columns span two drift shifts) and a 4000-step lattice (one shift per
+    group), orders 2..4: the fast ring kernel in parts of 256 columns with
+    a 5-row drift window.  Against the classic 1024-row kernel (k_bmaps0w):
+    density and profile within 2e-5 relative L1 after 24 steps; against
+    FP64: the bar; the profile against the FP64 Simpson sums of the
+    density rows."""
+    n = 1024
+    gap = 0.006 * P.derive(GridSize=n, StepsPerTs=2000, padding=2.0)["R_bend"]
+    specs = []
+    for spt, S, it in ((2000, 0.4, 4), (2000, 1.3, 2), (2000, 0.9, 3),
+                       (4000, 1.1, 4)):
+        p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0, VacuumGap=gap,
+                     S_csr=S)
+        specs.append((p, 0, p["Ib"], it, False))
+    z = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(specs[0][0]))
+    steps = 24
+    fast = make_batch(gpu_ctx, specs, {n: z})
+    tiles = fast.kernel_tiles()
+    assert tiles["k_bmaps0f"] > 0 and tiles["k_bmaps0w"] == 0, tiles
+    fast.step(steps)
+    monkeypatch.setenv("VFPS_RING_KERNEL", "classic")
+    classic = make_batch(gpu_ctx, specs, {n: z})
+    tiles = classic.kernel_tiles()
+    assert tiles["k_bmaps0f"] == 0 and tiles["k_bmaps0w"] > 0, tiles
+    classic.step(steps)
+    monkeypatch.delenv("VFPS_RING_KERNEL")
+    assert gpu_ctx.device_status() == 0
+    a, b = fast.download(), classic.download()
+    ws = np.asarray(oracle.simpson(n, specs[0][0]["axes"][0],
+                                   specs[0][0]["axes"][1], np.float32),
+                    np.float64)
+    for i, (p, ch, ib, it, cl) in enumerate(specs):
+        off, _ = fast.layout(i)
+        ga = a[off:off + n * n].reshape(n, n)
+        gb = b[off:off + n * n].reshape(n, n)
+        assert rel_l1(ga, gb) <= 2e-5, i
+        assert rel_l1(fast.profile(i), classic.profile(i)) <= 2e-5, i
+        sums = ga.astype(np.float64) @ ws
+        prof = np.asarray(fast.profile(i), np.float64)
+        assert np.abs(prof - sums).sum() / np.abs(sums).sum() <= 1e-6, i
+        assert np.abs(prof - sums).max() <= 1e-5 * sums.max(), i
+        ref = oracle_sim(p, ch, ib, z.data(), it=it, clamp=cl)
+        ref.step(steps, threads=os.cpu_count() or 1)
         assert rel_l1(ga, ref.density(0)) <= TOL, i
         assert rel_l1(fast.profile(i), ref.profile(0)) <= TOL, i

@@ -49,25 +49,29 @@ def window_walk(bunches, b, x0, rows, rb, off, ring, nthreads=128):
     n, hlo, hhi = bunches[b]
     seg = n // 8
     assert rows <= rb // 2
+    # 1024 rows: 5-row windows (256-thread CTAs, two groups of 4 parts)
+    depth = 5 if n >= 1024 else 4
+    if n >= 1024:
+        nthreads = 256
     rp = nthreads // seg
     per = -(-rows // rp)
     steps = -(-per // 4) * 4
     checked = 0
-    for sh in range(-hlo, hhi - 3 + 1):
+    for sh in range(-hlo, hhi - (depth - 1) + 1):
         for rl in range(rp):
             ra = rl * per
             xend = x0 + min(rows, ra + per)
             q = (x0 + ra + sh + off) % rb          # slot0
             win = []
-            for j in range(3):
+            for j in range(depth - 1):
                 win.append(q)
                 q = q + 1 if q + 1 < rb else 0
             for X in range(x0 + ra, x0 + ra + steps):
-                win.append(q)                      # row X + sh + 3
+                win.append(q)                      # row X + sh + depth - 1
                 q = q + 1 if q + 1 < rb else 0
                 assert all(0 <= w < rb for w in win)
                 if X < xend:
-                    for j in range(4):
+                    for j in range(depth):
                         assert ring.get(win[j]) == (b, X + sh + j), (
                             "window row", b, X, sh, j)
                         checked += 1
@@ -141,6 +145,7 @@ MIXES = {
     "narrow halos": [(64, 0, 3), (128, 1, 3), (256, 2, 4)] * 4,
     "wide halos": [(128, 6, 9), (256, 10, 12), (64, 3, 3)] * 3,
     "512 rows": [(512, 3, 4)] * 3 + [(512, 1, 3)] * 2,
+    "1024 rows": [(1024, 2, 5)] * 3 + [(1024, 1, 4)] * 2,
     "short tails": [(512, 1, 3), (256, 3, 4), (128, 2, 6)] * 2,
 }
 
@@ -158,7 +163,7 @@ def test_ring_staging_invariants(mix, tile_cells):
 
 
 @pytest.mark.parametrize("mix", ["scan 256", "narrow halos", "wide halos",
-                                 "512 rows", "short tails"])
+                                 "512 rows", "1024 rows", "short tails"])
 @pytest.mark.parametrize("tile_cells", [2048, 4096, 8192])
 def test_fast_ring_windows(mix, tile_cells):
     bunches = MIXES[mix]
