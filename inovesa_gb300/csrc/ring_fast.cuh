@@ -1,13 +1,13 @@
 // k_bmaps0f: chain 0 (the reference's loop, src/main.cpp:1034-1044:
-// wake kick, RF kick, drift, Fokker-Planck) for meshes of 64, 128, 256 and
-// 512 rows
-// whose lattice has the regular form of the benchmark's scans (checked on
-// the host, fast_ring_ok): every aligned group of 4 energy columns has one
-// drift shift, and the Fokker-Planck stencil of the lower half of the
-// energy axis spans offsets -2..1, that of the upper half -1..2 (the
-// cubic stencil of a mesh centred on the reference energy, whose last
-// lower column may take the upper form and reach -2..2; two-sided
-// stencils and no Fokker-Planck fit too).  Other lattices run on k_bmaps0.
+// wake kick, RF kick, drift, Fokker-Planck) for meshes of 64, 128, 256,
+// 512 and 1024 rows whose lattice has the regular form of the benchmark's
+// scans (checked on the host, fast_ring_ok): every aligned group of 4
+// energy columns has one drift shift (1024 rows: at most two adjacent
+// ones), and the Fokker-Planck stencil of the lower half of the energy
+// axis spans offsets -2..1, that of the upper half -1..2 (the cubic
+// stencil of a mesh centred on the reference energy, whose last lower
+// column may take the upper form and reach -2..2; two-sided stencils and
+// no Fokker-Planck fit too).  Other lattices run on k_bmaps0 / k_bmaps0w.
 //
 // Included by batch.cu after batch_kernels.cuh (shares its ring, tiles and
 // bulk-copy helpers).  Per tile of rows, as k_bmaps0:
@@ -22,12 +22,14 @@
 //           in packed FP32, Fokker-Planck with 4 taps (neighbour columns
 //           by shuffles), the new row to HBM and its Simpson sum; the row
 //           sums of 4 output rows leave in one reduce-scatter.
-// 512-row meshes: stage 1 gives a row to one warp (4 column groups per
-// lane); in stage 2 a pair of warps walks the rows, one warp per half of
-// the energy axis (two groups per lane, as a 256-row mesh), each warp
-// computing the drift of the two columns past its half that its
-// Fokker-Planck stencils reach; the two halves' row sums meet in shared
-// memory and are stored after the tile's next barrier.
+// 512- and 1024-row meshes: stage 1 gives a row to one warp (n/128 column
+// groups per lane); in stage 2 a group of n/256 warps walks the rows, one
+// warp per part of 256 columns (two groups per lane, as a 256-row mesh),
+// each warp computing the drift of the columns past its part that its
+// Fokker-Planck stencils reach from 2-column windows of its own; the
+// parts' row sums meet in shared memory and are stored after the tile's
+// next barrier.  1024 rows: 5-row drift windows (a group spanning two
+// shifts reads one more row) and 256-thread CTAs.
 #pragma once
 
 namespace {
