@@ -380,6 +380,54 @@ def config_plain_rotation(ctx, hbm):
             "cpu_sample": "%d solver steps, 1 thread" % k1}
 
 
+def bursting_params(ctx):
+    """The bursting bunch: 512x512, 4000 steps per period, S = 1.2,
+    parallel-plates CSR (g/R = 0.006) and a resistive wall (5.8e7 S/m):
+    its parameters, wake impedance and CSR impedance."""
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    n, spt, S = 512, 4000, 1.2
+    p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                 VacuumGap=0.006 * p0["R_bend"], S_csr=S,
+                 WallConductivity=5.8e7)
+    z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+    zr = V.makeImpedance(ctx, **P.csr_impedance_args(p))
+    return p, z, zr
+
+
+def bursting_batch(ctx, p, z, zr, currents):
+    """Bunches of the bursting lattice at the currents given (in units of
+    the threshold current's S), each with its CSR power every step."""
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    S = p["S_csr"]
+    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"] * c / S,
+                         impedance=0) for c in currents]
+    b = V.BunchBatch(ctx, descs, [z])
+    m = len(currents)
+    b.set_csr([zr], [0] * m, [p["fc"]] * m, [P.C / p["bl"]] * m,
+              every=1, capacity=8)
+    return b
+
+
+def uneven_batch(ctx):
+    """The uneven batch (uneven_workload's seed 4: 96 bunches, 2000 steps
+    per period) with one impedance per mesh size; also its (parameters,
+    order) list and sizes."""
+    from inovesa_gb300 import params as P
+    from inovesa_gb300 import vfps as V
+    ps, keys = uneven_workload(4, 96, 2000)
+    zs = {}
+    for k in keys:
+        pk = next(p for p, _ in ps if p["ps_bins"] == k)
+        zs[k] = V.makeImpedance(ctx, **P.wake_impedance_args(pk))
+    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"],
+                         impedance=keys.index(p["ps_bins"]), it=it)
+             for p, it in ps]
+    return V.BunchBatch(ctx, descs, [zs[k] for k in keys]), ps, keys
+
+
 def config_bursting(ctx, stream, hbm):
     """Bursting: 512x512, parallel-plates CSR (g/R = 0.006) + resistive
     wall (5.8e7 S/m), 4000 steps per period, S = 1.2, CSR power every step:
@@ -388,16 +436,10 @@ def config_bursting(ctx, stream, hbm):
     bunch every step; densities against FP64 after 200 steps."""
     import oracle
     from inovesa_gb300 import params as P
-    from inovesa_gb300 import vfps as V
-    n, spt, S = 512, 4000, 1.2
-    p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
-    p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
-                 VacuumGap=0.006 * p0["R_bend"], S_csr=S,
-                 WallConductivity=5.8e7)
+    p, z, zr = bursting_params(ctx)
+    S = p["S_csr"]
     total, warm = 200, 20
     rate, dens = plain_driver(p, 0, 4, False, total - warm, warm, csr=True)
-    z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
-    zr = V.makeImpedance(ctx, **P.csr_impedance_args(p))
     d = P.fill_desc(oracle.BunchDesc(), p, 0, Ib=p["Ib"], it=4)
     ref = oracle.Sim([d], Z=z.data(), dtype=np.float64)
     ref.step(total)
@@ -410,13 +452,7 @@ def config_bursting(ctx, stream, hbm):
            "accuracy_steps": total}
 
     def batch(currents):
-        descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"] * c / S,
-                             impedance=0) for c in currents]
-        b = V.BunchBatch(ctx, descs, [z])
-        m = len(currents)
-        b.set_csr([zr], [0] * m, [p["fc"]] * m, [P.C / p["bl"]] * m,
-                  every=1, capacity=8)
-        return b
+        return bursting_batch(ctx, p, z, zr, currents)
     b1 = batch([S])
     out["gpu_batched_one"] = timed_batch(b1, stream, 200, 10)
     bs = batch(list(np.geomspace(0.8, 1.6, 32)))
@@ -441,17 +477,8 @@ def config_uneven(ctx, stream, hbm, cores):
     the plain loop (C++ driver, one bunch of each size, weighted by the
     batch's mix), a host-core sample."""
     from inovesa_gb300 import params as P
-    from inovesa_gb300 import vfps as V
-    ps, keys = uneven_workload(4, 96, 2000)
+    b, ps, keys = uneven_batch(ctx)
     sizes = np.array([p["ps_bins"] for p, _ in ps])
-    zs = {}
-    for k in keys:
-        pk = next(p for p, _ in ps if p["ps_bins"] == k)
-        zs[k] = V.makeImpedance(ctx, **P.wake_impedance_args(pk))
-    descs = [P.fill_desc(V.BunchDesc(), p, 0, Ib=p["Ib"],
-                         impedance=keys.index(p["ps_bins"]), it=it)
-             for p, it in ps]
-    b = V.BunchBatch(ctx, descs, [zs[k] for k in keys])
     out = {"workload": "uneven batch: 96 bunches, meshes 128..1024 "
                        "(seeded), S~U(0.1,1.5), orders 2..4, 2000 "
                        "steps/period",
@@ -532,6 +559,11 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="timed steps only (for ncu): no e2e, plain loop or "
                          "CPU legs")
+    ap.add_argument("--workload", default="scan",
+                    choices=["scan", "uneven", "bursting32"],
+                    help="with --profile: the batch stepped (the current "
+                         "scan, the uneven 96-bunch batch or the 32-bunch "
+                         "512x512 bursting scan)")
     args = ap.parse_args()
     if args.profile:
         args.no_cpu = True
@@ -559,9 +591,15 @@ def main():
 
     p, gap, currents = workload_params()
     ctx = V.Context(local)
-    z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
-    batch = make_batch(ctx, p, currents, z)
-    batch.set_wake_mode(args.wake_mode)
+    if args.profile and args.workload == "uneven":
+        batch, _, _ = uneven_batch(ctx)
+    elif args.profile and args.workload == "bursting32":
+        batch = bursting_batch(ctx, *bursting_params(ctx),
+                               list(np.geomspace(0.8, 1.6, 32)))
+    else:
+        z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+        batch = make_batch(ctx, p, currents, z)
+        batch.set_wake_mode(args.wake_mode)
     cells = batch.cells
     stream = torch.cuda.ExternalStream(
         _lib.lib().vfps_stream(ctx.handle), device=local)
@@ -585,6 +623,10 @@ def main():
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if args.profile:
+        # the timed steps are the profiled range (ncu --profile-from-start
+        # off skips the set-up and the tile-size tuning)
+        torch.cuda.profiler.start()
     with ClockSampler(local) as clk:
         for e0, e1 in ev:
             flush_l2()
@@ -592,6 +634,8 @@ def main():
             batch.step(1)
             e1.record(stream)
         ev[-1][1].synchronize()
+    if args.profile:
+        torch.cuda.profiler.stop()
     ms = sum(e0.elapsed_time(e1) for e0, e1 in ev)
     torch.cuda.synchronize()
     if dist:
@@ -609,8 +653,12 @@ def main():
         sys.exit(3)
     if args.profile:
         if rank == 0:
-            print(json.dumps({"profile_run": True, "value": value,
-                              "ms_per_step": ms_step}), flush=True)
+            print(json.dumps({"profile_run": True,
+                              "workload": args.workload, "value": value,
+                              "ms_per_step": ms_step,
+                              "tile_rows": tile_rows,
+                              "kernel_tiles": batch.kernel_tiles()}),
+                  flush=True)
         return
 
     # back-to-back steps (8-step graphs, no flush): what a long run sees
