@@ -464,3 +464,35 @@ def test_fast_ring_kernel_1024(gpu_ctx, monkeypatch):
         ref.step(steps, threads=os.cpu_count() or 1)
         assert rel_l1(ga, ref.density(0)) <= TOL, i
         assert rel_l1(fast.profile(i), ref.profile(0)) <= TOL, i
+
+
+@pytest.mark.parametrize("tile_cells", ["2048", "12288"])
+def test_fast_ring_tile_sizes(gpu_ctx, monkeypatch, tile_cells):
+    """The fast ring kernel's 512- and 1024-row forms at the smallest and
+    largest tile sizes the autotuner tries (4-row tiles, where a group of
+    warps walks 2 rows and drops the other 2 of its 4-row step; 24- and
+    12-row tiles), a 512- and a 1024-row bunch in one batch: against the
+    classic kernels (at their own tiles) after 12 steps (2e-5 relative
+    L1)."""
+    monkeypatch.setenv("VFPS_TILE_CELLS", tile_cells)
+    specs, zs = [], {}
+    for n, spt, S, it in ((512, 4000, 1.1, 4), (1024, 2000, 0.7, 3)):
+        p0 = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0)
+        p = P.derive(GridSize=n, StepsPerTs=spt, padding=2.0,
+                     VacuumGap=0.006 * p0["R_bend"], S_csr=S)
+        specs.append((p, 0, p["Ib"], it, False))
+        zs[n] = V.makeImpedance(gpu_ctx, **P.wake_impedance_args(p))
+    fast = make_batch(gpu_ctx, specs, zs)
+    assert fast.kernel_tiles()["k_bmaps0f"] > 0
+    fast.step(12)
+    # the classic kernels at the autotuner's tiles (12288-cell tiles of a
+    # 1024-row mesh do not fit k_bmaps0w's shared memory)
+    monkeypatch.delenv("VFPS_TILE_CELLS")
+    monkeypatch.setenv("VFPS_RING_KERNEL", "classic")
+    classic = make_batch(gpu_ctx, specs, zs)
+    assert classic.kernel_tiles()["k_bmaps0f"] == 0
+    classic.step(12)
+    assert gpu_ctx.device_status() == 0
+    for i in range(len(specs)):
+        assert rel_l1(fast.density(i), classic.density(i)) <= 2e-5, i
+        assert rel_l1(fast.profile(i), classic.profile(i)) <= 2e-5, i
