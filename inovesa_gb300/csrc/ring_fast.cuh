@@ -435,8 +435,9 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             // per output row (segments past the tile's rows start further
             // on: reduced modulo the ring)
             auto slot0 = [&](int x) {
-                int q = (x + mc.off) % rb;
-                return q < 0 ? q + rb : q;
+                // x + off lies in [-rb, 2 rb): one step reduces it
+                const int q = x + mc.off;
+                return q < 0 ? q + rb : (q >= rb ? q - rb : q);
             };
             int oA = slot0(x0 + ra + shA) * rs + APAD + yA;
             int oB = slot0(x0 + ra + shB) * rs + APAD + yB;
@@ -574,8 +575,9 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
             float* psum = part + (k & 1) * PARTS * (rb >> 1)
                           + h * (rb >> 1) - x0;
             auto slot0 = [&](int x) {
-                int q = (x + mc.off) % rb;
-                return q < 0 ? q + rb : q;
+                // x + off lies in [-rb, 2 rb): one step reduces it
+                const int q = x + mc.off;
+                return q < 0 ? q + rb : (q >= rb ? q - rb : q);
             };
             auto next = [&](int& o) {
                 o += rs;

@@ -61,7 +61,10 @@ def window_walk(bunches, b, x0, rows, rb, off, ring, nthreads=128):
         for rl in range(rp):
             ra = rl * per
             xend = x0 + min(rows, ra + per)
-            q = (x0 + ra + sh + off) % rb          # slot0
+            raw = x0 + ra + sh + off
+            # slot0's reduction: one conditional step each way suffices
+            assert -rb <= raw < 2 * rb, ("slot0 range", raw, rb)
+            q = raw + rb if raw < 0 else (raw - rb if raw >= rb else raw)
             win = []
             for j in range(depth - 1):
                 win.append(q)
