@@ -522,15 +522,20 @@ def config_warm_start(ctx):
     return res
 
 
-def config_scan_rotation(ctx, stream, hbm, p, currents, z):
-    """The current scan of the headline on the rotation chain (cubic
-    RotationMap, wake kick, Fokker-Planck; the batched k_bmaps1): rate,
-    kernel times and the maps kernel's HBM fraction."""
+def rotation_scan_batch(ctx, p, currents, z):
+    """The headline's current scan on the rotation chain (chain 1)."""
     from inovesa_gb300 import params as P
     from inovesa_gb300 import vfps as V
     descs = [P.fill_desc(V.BunchDesc(), p, 1, Ib=float(ib), impedance=0)
              for ib in currents]
-    b = V.BunchBatch(ctx, descs, [z])
+    return V.BunchBatch(ctx, descs, [z])
+
+
+def config_scan_rotation(ctx, stream, hbm, p, currents, z):
+    """The current scan of the headline on the rotation chain (cubic
+    RotationMap, wake kick, Fokker-Planck; the batched k_bmaps1): rate,
+    kernel times and the maps kernel's HBM fraction."""
+    b = rotation_scan_batch(ctx, p, currents, z)
     out = {"workload": "the headline's 256-bunch scan on the rotation "
                        "chain (cubic RotationMap, wake kick, "
                        "Fokker-Planck)",
@@ -560,10 +565,11 @@ def main():
                     help="timed steps only (for ncu): no e2e, plain loop or "
                          "CPU legs")
     ap.add_argument("--workload", default="scan",
-                    choices=["scan", "uneven", "bursting32"],
+                    choices=["scan", "uneven", "bursting32", "rotation"],
                     help="with --profile: the batch stepped (the current "
-                         "scan, the uneven 96-bunch batch or the 32-bunch "
-                         "512x512 bursting scan)")
+                         "scan, the uneven 96-bunch batch, the 32-bunch "
+                         "512x512 bursting scan or the current scan on the "
+                         "rotation chain)")
     args = ap.parse_args()
     if args.profile:
         args.no_cpu = True
@@ -593,6 +599,9 @@ def main():
     ctx = V.Context(local)
     if args.profile and args.workload == "uneven":
         batch, _, _ = uneven_batch(ctx)
+    elif args.profile and args.workload == "rotation":
+        z = V.makeImpedance(ctx, **P.wake_impedance_args(p))
+        batch = rotation_scan_batch(ctx, p, currents, z)
     elif args.profile and args.workload == "bursting32":
         batch = bursting_batch(ctx, *bursting_params(ctx),
                                list(np.geomspace(0.8, 1.6, 32)))

@@ -2075,20 +2075,59 @@ __host__ __device__ inline Smem1 smem1(int n, int nr, int rows)
     return L;
 }
 
+// Lagrange weights (calcCoefficiants, src/SM/SourceMap.cpp:142-170) of two
+// fractions at once, in packed FP32: each component rounds as the scalar
+// form's fmul / fadd / fsub (a - b computed as a + (-b), the same bits)
+template <int IT>
+__device__ __forceinline__ void coefficients2(float2* ic, float2 f)
+{
+    const float2 one = make_float2(1.f, 1.f);
+    const float2 mone = make_float2(-1.f, -1.f);
+    if (IT == 2) {
+        ic[0] = __fadd2_rn(one, make_float2(-f.x, -f.y));
+        ic[1] = f;
+    } else if (IT == 3) {
+        const float2 half = make_float2(0.5f, 0.5f);
+        ic[0] = __fmul2_rn(__fmul2_rn(f, __fadd2_rn(f, mone)), half);
+        const float2 ff = __fmul2_rn(f, f);
+        ic[1] = __fadd2_rn(one, make_float2(-ff.x, -ff.y));
+        ic[2] = __fmul2_rn(__fmul2_rn(f, __fadd2_rn(f, one)), half);
+    } else {
+        const float2 fm1 = __fadd2_rn(f, mone);
+        const float2 fm2 = __fadd2_rn(f, make_float2(-2.f, -2.f));
+        const float2 fp1 = __fadd2_rn(f, one);
+        const float2 tmf = __fadd2_rn(make_float2(2.f, 2.f),
+                                      make_float2(-f.x, -f.y));
+        const float s6 = static_cast<float>(-1. / 6.);
+        const float p6 = static_cast<float>(1. / 6.);
+        ic[0] = __fmul2_rn(__fmul2_rn(__fmul2_rn(fm1, fm2), f),
+                           make_float2(s6, s6));
+        ic[1] = __fmul2_rn(__fmul2_rn(__fmul2_rn(fp1, fm1), fm2),
+                           make_float2(0.5f, 0.5f));
+        ic[2] = __fmul2_rn(__fmul2_rn(__fmul2_rn(tmf, f), fp1),
+                           make_float2(0.5f, 0.5f));
+        ic[3] = __fmul2_rn(__fmul2_rn(__fmul2_rn(f, fp1), fm1),
+                           make_float2(p6, p6));
+    }
+}
+
 // The rotation (src/SM/RotationMap.cpp:97-260) of a tile's rows from the
 // staged rows A ([nr][n + 8], 4 zero columns each side) into Bs
 // ([rows][n + ROWPAD], slot j of row r holds mesh column j + the row's
 // wake kick shift), for interpolation with IT points per axis (the
 // reference's calcCoefficiants, src/SM/SourceMap.cpp:142-170) and, when
-// CLAMP, the CPU path's clamp to the 2x2 nearest taps.  A warp per row,
-// lanes across the slots.
-template <int IT, bool CLAMP>
+// CLAMP, the CPU path's clamp to the 2x2 nearest taps.  A warp per row;
+// each lane computes the slots j and j + 32 together: their source
+// coordinates, Lagrange weights and tap sums in packed FP32 (each
+// component rounds as the scalar operation), their taps and clamps one
+// by one.  NC: the mesh size as a constant (0: the bunch's).
+template <int IT, bool CLAMP, int NC>
 __device__ __forceinline__ void rotate_rows(
     const BDev& B, int x0, int rows, int hlo, const float* __restrict__ tabs,
     const float* __restrict__ din, float fac, const float* A, float* Bs,
     const RowStencil* S, const float* snp, const float* csp)
 {
-    const int n = int(B.n);
+    const int n = NC ? NC : int(B.n);
     const int astride = n + 8;
     const int bstride = n + ROWPAD;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -2097,49 +2136,72 @@ __device__ __forceinline__ void rotate_rows(
     const float* qv = tabs + B.tab_off + TAB_Q * n;
     const float cell0 = CLAMP ? din[B.dens_off] * fac : 0.f;
     const float inv_dq = 1.f / B.dq, inv_dp = 1.f / B.dp;
-    const float zbq = B.zbq, zbp = B.zbp;
+    const float2 idq2 = make_float2(inv_dq, inv_dq);
+    const float2 idp2 = make_float2(inv_dp, inv_dp);
+    const float2 zbq2 = make_float2(B.zbq, B.zbq);
+    const float2 zbp2 = make_float2(B.zbp, B.zbp);
     // staged row of tap i1 of base x1: x1 + i1 - h - (x0 - hlo)
     const int row0 = hlo - h - x0;
     for (int r = warp; r < rows; r += NW) {
         const float q = qv[x0 + r];
         const float cq = __fmul_rn(B.cs, q), sq = __fmul_rn(B.sn, q);
+        const float2 cq2 = make_float2(cq, cq), sq2 = make_float2(sq, sq);
         const int sh = S[r].shift0;
         float* brow = Bs + size_t(r) * bstride;
-        for (int j = lane; j < bstride; j += 32) {
-            const int y0 = j + sh;            // mesh column of this slot
-            float v = 0.f;
-            if (unsigned(y0) < unsigned(n)) {
-                const float x1r = __fmaf_rn(__fsub_rn(cq, snp[y0]), inv_dq,
-                                            zbq);
-                const float y1r = __fmaf_rn(__fadd_rn(sq, csp[y0]), inv_dp,
-                                            zbp);
-                int x1 = 0, y1 = 0;
-                float xf, yf;
-                const bool okx = base_index(x1r, B.n, &x1, &xf);
-                const bool oky = base_index(y1r, B.n, &y1, &yf);
-                const bool ok = okx && oky;
-                float tap[IT][IT];
-                if (ok) {
-                    float icq[4], icp[4];
-                    coefficients(icq, xf, IT);
-                    coefficients(icp, yf, IT);
-                    const float* srow = A + size_t(x1 + row0) * astride
-                                        + (y1 - h + 4);
+        for (int j = lane; j < bstride; j += 64) {
+            const int jb = j + 32;
+            const bool hasb = jb < bstride;
+            const int ya = j + sh, yb = jb + sh;   // mesh columns
+            const bool ina = unsigned(ya) < unsigned(n);
+            const bool inb = hasb && unsigned(yb) < unsigned(n);
+            const int ca = ina ? ya : 0, cb = inb ? yb : 0;
+            const float2 sn2 = make_float2(-snp[ca], -snp[cb]);
+            const float2 cs2 = make_float2(csp[ca], csp[cb]);
+            const float2 x1r = __ffma2_rn(__fadd2_rn(cq2, sn2), idq2, zbq2);
+            const float2 y1r = __ffma2_rn(__fadd2_rn(sq2, cs2), idp2, zbp2);
+            int x1a = 0, y1a = 0, x1b = 0, y1b = 0;
+            float2 xf, yf;
+            const bool oka = base_index(x1r.x, n, &x1a, &xf.x)
+                             & base_index(y1r.x, n, &y1a, &yf.x) & ina;
+            const bool okb = base_index(x1r.y, n, &x1b, &xf.y)
+                             & base_index(y1r.y, n, &y1b, &yf.y) & inb;
+            float2 icq[4], icp[4];
+            coefficients2<IT>(icq, xf);
+            coefficients2<IT>(icp, yf);
+            float ta[IT][IT], tb[IT][IT];
+            // the taps of each slot (a slot without a source cell reads
+            // none: zeros)
+            {
+                const float* sa = A + size_t(x1a + row0) * astride
+                                  + (y1a - h + 4);
+                const float* sb = A + size_t(x1b + row0) * astride
+                                  + (y1b - h + 4);
 #pragma unroll
-                    for (int i1 = 0; i1 < IT; i1++) {
-                        const float* rr = srow + i1 * astride;
-                        float rv = 0.f;
+                for (int i1 = 0; i1 < IT; i1++) {
 #pragma unroll
-                        for (int j1 = 0; j1 < IT; j1++) {
-                            tap[i1][j1] = rr[j1];
-                            rv = fmaf(tap[i1][j1], icp[j1], rv);
-                        }
-                        v = fmaf(rv, icq[i1], v);
+                    for (int j1 = 0; j1 < IT; j1++) {
+                        ta[i1][j1] = oka ? sa[i1 * astride + j1] : 0.f;
+                        tb[i1][j1] = okb ? sb[i1 * astride + j1] : 0.f;
                     }
                 }
-                if (CLAMP) {
-                    // 2x2 nearest taps; taps off the mesh read cell (0,0),
-                    // as the CPU path's clamp does
+            }
+            float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i1 = 0; i1 < IT; i1++) {
+                float2 rv = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int j1 = 0; j1 < IT; j1++) {
+                    rv = __ffma2_rn(make_float2(ta[i1][j1], tb[i1][j1]),
+                                    icp[j1], rv);
+                }
+                v = __ffma2_rn(rv, icq[i1], v);
+            }
+            float va = oka ? v.x : 0.f, vb = okb ? v.y : 0.f;
+            if (CLAMP) {
+                // 2x2 nearest taps; taps off the mesh read cell (0,0),
+                // as the CPU path's clamp does
+                auto clamp1 = [&](float val, bool ok, bool in, int x1,
+                                  int y1, const float (&tap)[IT][IT]) {
                     float hi = FLT_MIN, lo = FLT_MAX;
 #pragma unroll
                     for (int i1 = 1; i1 <= 2; i1++) {
@@ -2156,11 +2218,17 @@ __device__ __forceinline__ void rotate_rows(
                             lo = (sv < lo) ? sv : lo;
                         }
                     }
-                    const float tmin = (v < hi) ? v : hi;
-                    v = (tmin < lo) ? lo : tmin;
-                }
+                    const float tmin = (val < hi) ? val : hi;
+                    const float c = (tmin < lo) ? lo : tmin;
+                    return in ? c : 0.f;
+                };
+                va = clamp1(va, oka, ina, x1a, y1a, ta);
+                vb = clamp1(vb, okb, inb, x1b, y1b, tb);
             }
-            brow[j] = v;
+            brow[j] = va;
+            if (hasb) {
+                brow[jb] = vb;
+            }
         }
     }
 }
@@ -2264,24 +2332,47 @@ k_bmaps1(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     // the bunch's: one instance each, chosen once per tile)
     {
         const bool clamp = B.flags & F_CLAMP;
-        switch (it) {
-        case 2:
-            rotate_rows<2, false>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
-                                  S, snp, csp);
-            break;
-        case 3:
-            rotate_rows<3, false>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
-                                  S, snp, csp);
-            break;
-        default:
-            if (clamp) {
-                rotate_rows<4, true>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
-                                     S, snp, csp);
-            } else {
-                rotate_rows<4, false>(B, x0, rows, hlo, tabs, din, fac, A, Bs,
-                                      S, snp, csp);
+        // 256-row meshes (the benchmark's) with the mesh size a constant
+        if (n == 256) {
+            switch (it) {
+            case 2:
+                rotate_rows<2, false, 256>(B, x0, rows, hlo, tabs, din, fac,
+                                           A, Bs, S, snp, csp);
+                break;
+            case 3:
+                rotate_rows<3, false, 256>(B, x0, rows, hlo, tabs, din, fac,
+                                           A, Bs, S, snp, csp);
+                break;
+            default:
+                if (clamp) {
+                    rotate_rows<4, true, 256>(B, x0, rows, hlo, tabs, din,
+                                              fac, A, Bs, S, snp, csp);
+                } else {
+                    rotate_rows<4, false, 256>(B, x0, rows, hlo, tabs, din,
+                                               fac, A, Bs, S, snp, csp);
+                }
+                break;
             }
-            break;
+        } else {
+            switch (it) {
+            case 2:
+                rotate_rows<2, false, 0>(B, x0, rows, hlo, tabs, din, fac, A,
+                                         Bs, S, snp, csp);
+                break;
+            case 3:
+                rotate_rows<3, false, 0>(B, x0, rows, hlo, tabs, din, fac, A,
+                                         Bs, S, snp, csp);
+                break;
+            default:
+                if (clamp) {
+                    rotate_rows<4, true, 0>(B, x0, rows, hlo, tabs, din, fac,
+                                            A, Bs, S, snp, csp);
+                } else {
+                    rotate_rows<4, false, 0>(B, x0, rows, hlo, tabs, din,
+                                             fac, A, Bs, S, snp, csp);
+                }
+                break;
+            }
         }
     }
     __syncthreads();
