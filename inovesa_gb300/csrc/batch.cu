@@ -220,7 +220,7 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
         b->beams.p, b->members.p,
         CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
                b->csr_every, b->csr_cap, b->nb, b->csrpart.p, b->csrdone.p},
-        b->ctx->d_status, tc ? 1 : 0);
+        b->ctx->d_status, tc ? 1 : 0, b->nwblk == b->nb ? 1 : 0);
     VFPS_LAUNCHED();
     mark(1);
     // programmatic dependent launch of the first ring kernel: its CTAs zero

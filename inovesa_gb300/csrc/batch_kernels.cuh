@@ -331,7 +331,7 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
         double* __restrict__ filling, unsigned long long* __restrict__ tickets,
         const BeamDev* __restrict__ beams,
         const uint32_t* __restrict__ members, CsrRec csr,
-        int* __restrict__ status, int wake_ready)
+        int* __restrict__ status, int wake_ready, int block_per_bunch)
 {
     extern __shared__ float4 wsm4[];
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
@@ -339,7 +339,10 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     __shared__ unsigned long long ticket_s;
     // the maps kernel that follows may start its prologue now
     pdl_trigger();
-    const uint2 blk = wblk[blockIdx.x];
+    // one block per bunch (no mesh wider than a block): CTA i is bunch i,
+    // and its record loads do not wait for the block list
+    const uint2 blk = block_per_bunch ? make_uint2(blockIdx.x, 0u)
+                                      : wblk[blockIdx.x];
     const uint32_t b = blk.x;
     const BDev B = bd[b];
     const int n = int(B.n);
