@@ -82,7 +82,8 @@ struct vfps_batch {
     // k_bwake's CTAs: (bunch, first row) of each block of rows
     DevBuf<uint2> wblk;
     uint32_t nwblk = 0;
-    // step tickets: every k_bwake CTA takes one, so step = tickets / nwblk
+    // step counters: one per k_bwake CTA, which advances its own once per
+    // step (no two CTAs share one)
     DevBuf<unsigned long long> tickets;
     int cur = 0;               // buffer holding the current state
     size_t smem[TL_COUNT] = {};
@@ -603,9 +604,9 @@ int autotune(vfps_batch* b)
                               cudaMemcpyDeviceToDevice, st));
     VFPS_CUDA(cudaMemcpyAsync(sp.p, b->prof[b->cur].p, sp.bytes(),
                               cudaMemcpyDeviceToDevice, st));
-    unsigned long long saved = 0;
-    VFPS_CUDA(cudaMemcpyAsync(&saved, b->tickets.p, sizeof(saved),
-                              cudaMemcpyDeviceToHost, st));
+    DevBuf<unsigned long long> saved(b->tickets.n);
+    VFPS_CUDA(cudaMemcpyAsync(saved.p, b->tickets.p, saved.bytes(),
+                              cudaMemcpyDeviceToDevice, st));
     VFPS_CUDA(cudaStreamSynchronize(st));
     const int cands[] = {2048, 3072, 4096, 6144, 8192, 12288};
     int best = 4096;
@@ -644,8 +645,8 @@ int autotune(vfps_batch* b)
                               cudaMemcpyDeviceToDevice, st));
     VFPS_CUDA(cudaMemcpyAsync(b->prof[b->cur].p, sp.p, sp.bytes(),
                               cudaMemcpyDeviceToDevice, st));
-    VFPS_CUDA(cudaMemcpyAsync(b->tickets.p, &saved, sizeof(saved),
-                              cudaMemcpyHostToDevice, st));
+    VFPS_CUDA(cudaMemcpyAsync(b->tickets.p, saved.p, saved.bytes(),
+                              cudaMemcpyDeviceToDevice, st));
     VFPS_CUDA(cudaStreamSynchronize(st));
     {
         std::lock_guard<std::mutex> lk(g_tune_mu);
@@ -1243,7 +1244,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
         VFPS_CUDA(cudaMemsetAsync(b->wake.p, 0, b->wake.bytes(), st));
         b->factor.alloc(nb);
         b->filling.alloc(nb);
-        b->tickets.alloc(1);
+        b->tickets.alloc(b->nwblk);
         VFPS_CUDA(cudaMemsetAsync(b->tickets.p, 0, b->tickets.bytes(), st));
         VFPS_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
         VFPS_CUDA(cudaEventCreateWithFlags(&b->fork,

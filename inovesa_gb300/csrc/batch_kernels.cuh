@@ -318,9 +318,9 @@ __device__ __forceinline__ void beam_wake_rows(
 // the block's rows, charge integral, renormalisation factor and, for chain 0,
 // both y-kick stencils of the block's rows.  Every CTA of a bunch sums the
 // whole profile's charge (the same bits); the first one stores it.  The
-// step number comes from a 64-bit ticket that every CTA takes once per
-// step (one ticket per CTA and step), so no CTA has to wait for the others
-// or reset anything.
+// step number is the CTA's own 64-bit counter, which it advances once per
+// step (the steps run in stream order, and no other CTA touches it), so no
+// CTA waits for another or contends for a shared counter.
 __global__ void __launch_bounds__(THREADS)
 k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
         const float* __restrict__ tabs,
@@ -352,7 +352,7 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     // per 8 puts the 32 lanes of the wake sum (rows 8 apart) on 32 banks
     float* W = P + n;
     if (threadIdx.x == 0) {
-        ticket_s = atomicAdd(tickets, 1ull);
+        ticket_s = tickets[blockIdx.x]++;
     }
     for (int i = threadIdx.x; i < n; i += THREADS) {
         P[i] = pin[B.prof_off + i];
@@ -418,7 +418,7 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
                    __shfl_xor_sync(0xffffffffu, tot.lo, o)};
         tot = ff_add(tot, t);
     }
-    const unsigned step = static_cast<unsigned>(ticket_s / gridDim.x);
+    const unsigned step = static_cast<unsigned>(ticket_s);
     const bool renorm_now = B.renorm > 0 && (step % unsigned(B.renorm)) == 0;
     float fac = 1.f;
     if (renorm_now && B.fillset > 0) {
