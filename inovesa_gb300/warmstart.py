@@ -8,8 +8,8 @@ between equilibria this solver produced and that state.
 
 The proposal enters the solver as initial data (the reference's
 PhaseSpace data argument, inc/PS/PhaseSpace.hpp:54-61, the hook of
-InitialDistFile in src/main.cpp:469-525); the solver stays the judge: a
-bunch counts as converged when the relative L1 change of its profile over
+InitialDistFile in src/main.cpp:469-525); the solver decides whether a
+start was good: a bunch counts as converged when the relative L1 change of its profile over
 one synchrotron period falls below a tolerance, and the warm-started and
 the Gaussian-started runs must reach the same equilibrium.
 
