@@ -38,7 +38,7 @@ struct __align__(16) BDev {     // 96 bytes: vector loads of its fields
     uint32_t dens_off, prof_off, tab_off, st_off;
     uint32_t fp_off, wt_off, nmax, rot_h;
     int32_t renorm, halo_lo, halo_hi;
-    uint32_t dw_off;               // drift planes (chain 0, n <= 256)
+    uint32_t dw_off;               // drift, Fokker-Planck planes (ring kernels)
     float wakescale, fillset, dq, dp;
     float zbq, zbp, cs, sn;
 };
