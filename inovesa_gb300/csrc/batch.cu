@@ -214,14 +214,33 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
             b->wake.p, b->ctx->d_status);
         VFPS_LAUNCHED();
     }
-    k_bwake<<<b->nwblk, THREADS, wsm, st>>>(
-        b->bd.p, b->wblk.p, b->tabs.p, b->wt.p, b->st.p, b->prof[from].p,
-        b->wake.p, b->rinfo.p, b->rinfo7.p, b->factor.p, b->filling.p,
-        b->tickets.p,
-        b->beams.p, b->members.p,
-        CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
-               b->csr_every, b->csr_cap, b->nb, b->csrpart.p, b->csrdone.p},
-        b->ctx->d_status, tc ? 1 : 0, b->nwblk == b->nb ? 1 : 0);
+    {
+        // a programmatic dependent of the previous step's maps kernel (when
+        // that is the last kernel on this stream): the launch overlaps that
+        // kernel's end, and k_bwake waits for it before it reads or writes
+        // anything the maps kernel touches
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cudaLaunchConfig_t c = {};
+        c.gridDim = dim3(b->nwblk);
+        c.blockDim = dim3(THREADS);
+        c.dynamicSmemBytes = wsm;
+        c.stream = st;
+        c.attrs = at;
+        c.numAttrs = tc ? 0 : 1;
+        VFPS_CUDA(cudaLaunchKernelEx(
+            &c, k_bwake, (const BDev*)b->bd.p, (const uint2*)b->wblk.p,
+            (const float*)b->tabs.p, (const float*)b->wt.p,
+            (const RowStencil*)b->st.p, (const float*)b->prof[from].p,
+            b->wake.p, b->rinfo.p, b->rinfo7.p, b->factor.p, b->filling.p,
+            b->tickets.p, (const BeamDev*)b->beams.p,
+            (const uint32_t*)b->members.p,
+            CsrRec{b->csrk.p, b->csroff.p, b->csrpow.p, b->csrsteps.p,
+                   b->csr_every, b->csr_cap, b->nb, b->csrpart.p,
+                   b->csrdone.p},
+            b->ctx->d_status, tc ? 1 : 0, b->nwblk == b->nb ? 1 : 0));
+    }
     VFPS_LAUNCHED();
     mark(1);
     // programmatic dependent launch of the first ring kernel: its CTAs zero

@@ -337,8 +337,6 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     float* P = reinterpret_cast<float*>(wsm4);      // [n]
     __shared__ float2 red[32];
     __shared__ unsigned long long ticket_s;
-    // the maps kernel that follows may start its prologue now
-    pdl_trigger();
     // one block per bunch (no mesh wider than a block): CTA i is bunch i,
     // and its record loads do not wait for the block list
     const uint2 blk = block_per_bunch ? make_uint2(blockIdx.x, 0u)
@@ -351,12 +349,6 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     // W[k + k/8] = w[(k - (n-1)) mod nmax] for k < 2n - 1: one pad entry
     // per 8 puts the 32 lanes of the wake sum (rows 8 apart) on 32 banks
     float* W = P + n;
-    if (threadIdx.x == 0) {
-        ticket_s = tickets[blockIdx.x]++;
-    }
-    for (int i = threadIdx.x; i < n; i += THREADS) {
-        P[i] = pin[B.prof_off + i];
-    }
     const bool has_wake = B.flags & F_WAKE;
     // wake_ready: the tensor-core kernel has written this step's wake
     const bool sum_here = has_wake && !wake_ready;
@@ -375,6 +367,19 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     RowStencil sb0 = {};
     if (B.chain == 0 && x0 < R) {
         sb0 = rf[xr0 + x0];
+    }
+    // the records and tables above do not change between steps; launched
+    // as a programmatic dependent of the previous step's maps kernel, the
+    // CTA reads them while that kernel ends, and waits for it here before
+    // it reads the profiles or writes anything.  Then the maps kernel that
+    // follows may start its prologue
+    pdl_wait();
+    pdl_trigger();
+    if (threadIdx.x == 0) {
+        ticket_s = tickets[blockIdx.x]++;
+    }
+    for (int i = threadIdx.x; i < n; i += THREADS) {
+        P[i] = pin[B.prof_off + i];
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

@@ -831,6 +831,8 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     if (bad && threadIdx.x == 0) {
         atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
     }
+    // the next step's k_bwake may launch once every CTA is here
+    pdl_trigger();
 }
 
 }  // namespace
