@@ -247,8 +247,9 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     // their rings, set up their barriers and start the bulk copies of their
     // first density rows while k_bwake runs, then wait for it to finish
     // (griddepcontrol.wait) before they read its stencils or write device
-    // memory.  Only ring kernels are launched so: k_bwake CTAs
-    // launched early crowd onto the SMs that finish first, which is slower.
+    // memory.  (The fast ring kernel lets the next k_bwake launch only at
+    // its end: k_bwake CTAs launched earlier crowd onto the SMs that finish
+    // first, which was measured slower.)
     cudaLaunchAttribute pdl[1];
     pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
     pdl[0].val.programmaticStreamSerializationAllowed = 1;
