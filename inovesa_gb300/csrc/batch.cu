@@ -113,8 +113,11 @@ struct vfps_batch {
     uint32_t csr_every = 0, csr_cap = 0;
     DevBuf<float> tplanes;
     DevBuf<TcGroup> tcg;
-    DevBuf<uint32_t> tclist;
+    DevBuf<uint2> tclist;      // per tile member: profile offset, scaling
     uint32_t tc_groups = 0;
+    bool tc_ok = true;     // every wake mesh fits the tensor-core kernel
+    uint32_t tc_n = 0;     // the widest of them
+    uint32_t tc_smem = 0;  // k_wake_tc's shared memory for all of them
     // a second stream for the maps kernels of the other mesh classes, which
     // run next to the first ring kernel (fork after k_bwake, join before
     // the step ends)
@@ -208,9 +211,9 @@ void launch_step(vfps_batch* b, int from, cudaEvent_t* ev = nullptr)
     mark(0);
     const bool tc = b->wake_tc && b->tc_groups > 0;
     if (tc) {
-        const dim3 grid((b->max_n + TC_M - 1) / TC_M, b->tc_groups);
-        k_wake_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(
-            b->bd.p, b->tcg.p, b->tclist.p, b->tplanes.p, b->prof[from].p,
+        const dim3 grid((b->tc_n + TC_M - 1) / TC_M, b->tc_groups);
+        k_wake_tc<<<grid, TC_THREADS, b->tc_smem, st>>>(
+            b->tcg.p, b->tclist.p, b->tplanes.p, b->prof[from].p,
             b->wake.p, b->ctx->d_status);
         VFPS_LAUNCHED();
     }
@@ -1199,7 +1202,7 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             }
             std::vector<float> tp;
             std::vector<TcGroup> groups;
-            std::vector<uint32_t> tl;
+            std::vector<uint2> tl;
             std::map<std::pair<uint32_t, uint32_t>, uint32_t> t_at;
             std::map<std::pair<uint32_t, uint32_t>, std::vector<uint32_t>>
                 members;
@@ -1215,15 +1218,40 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                 }
                 t_at[key] = static_cast<uint32_t>(tp.size());
                 const uint32_t nn = B.n, nmax = B.nmax;
+                if (nn % TC_K != 0 || nn > uint32_t(TC_MAX_N)) {
+                    b->tc_ok = false;   // no tensor-core wake for this batch
+                    continue;
+                }
+                b->tc_n = std::max(b->tc_n, nn);
+                b->tc_smem = std::max(b->tc_smem, tc_smem(int(nn)));
                 const float* w = wt_host.data() + B.wt_off;
-                const size_t hi0 = tp.size();
-                tp.resize(hi0 + 2 * size_t(nn) * nn);
-                for (uint32_t x = 0; x < nn; x++) {
-                    for (uint32_t m = 0; m < nn; m++) {
-                        const float v = w[(x + nmax - m) % nmax];
-                        const float h = tf32_hi(v);
-                        tp[hi0 + size_t(x) * nn + m] = h;
-                        tp[hi0 + size_t(nn) * nn + size_t(x) * nn + m] = v - h;
+                // the shared-memory images of every (row tile, chunk):
+                // T[x][m] at row r = x mod 128, chunk c of 4, element e,
+                // stored at r * 32 + 4 (c ^ (r & 7)) + e; hi plane, then lo
+                const uint32_t mtn = (nn + TC_M - 1) / TC_M, nkc = nn / TC_K;
+                const size_t at0 = tp.size();
+                tp.resize(at0 + size_t(mtn) * nkc * 2 * TC_IMG_FLOATS, 0.f);
+                for (uint32_t mt = 0; mt < mtn; mt++) {
+                    for (uint32_t kc = 0; kc < nkc; kc++) {
+                        float* hi = tp.data() + at0
+                                    + (size_t(mt) * nkc + kc) * 2
+                                          * TC_IMG_FLOATS;
+                        float* lo = hi + TC_IMG_FLOATS;
+                        for (uint32_t r = 0; r < uint32_t(TC_M); r++) {
+                            const uint32_t x = mt * TC_M + r;
+                            if (x >= nn) {
+                                break;
+                            }
+                            for (uint32_t k = 0; k < uint32_t(TC_K); k++) {
+                                const uint32_t m = kc * TC_K + k;
+                                const float v = w[(x + nmax - m) % nmax];
+                                const float h = tf32_hi(v);
+                                const uint32_t at =
+                                    r * TC_K + 4 * ((k / 4) ^ (r & 7)) + k % 4;
+                                hi[at] = h;
+                                lo[at] = v - h;
+                            }
+                        }
                     }
                 }
             }
@@ -1236,8 +1264,12 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
                     g.nbt = static_cast<uint32_t>(
                         std::min<size_t>(TC_N, idx.size() - j));
                     g.list_off = static_cast<uint32_t>(tl.size());
-                    tl.insert(tl.end(), idx.begin() + j,
-                              idx.begin() + j + g.nbt);
+                    for (size_t u = j; u < j + g.nbt; u++) {
+                        const BDev& Bm = b->hb[idx[u]];
+                        uint32_t sc;
+                        std::memcpy(&sc, &Bm.wakescale, sizeof(sc));
+                        tl.push_back(make_uint2(Bm.prof_off, sc));
+                    }
                     groups.push_back(g);
                 }
             }
@@ -1245,9 +1277,11 @@ extern "C" int vfps_batch_create(vfps_ctx* ctx, uint32_t nb,
             put(b->tplanes, tp);
             put(b->tcg, groups);
             put(b->tclist, tl);
-            VFPS_CUDA(cudaFuncSetAttribute(
-                k_wake_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                static_cast<int>(TC_SMEM)));
+            if (b->tc_ok && b->tc_n > 0) {
+                VFPS_CUDA(cudaFuncSetAttribute(
+                    k_wake_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    static_cast<int>(b->tc_smem)));
+            }
         }
         put(b->row_bunch, row_bunch);
         for (int k = 0; k < 2; k++) {
@@ -1859,7 +1893,8 @@ extern "C" int vfps_batch_get_csr(vfps_batch* b, float* power,
 
 extern "C" int vfps_batch_set_wake_mode(vfps_batch* b, int mode)
 {
-    if (!b || (mode != 0 && mode != 1) || (mode == 1 && b->coupled)) {
+    if (!b || (mode != 0 && mode != 1)
+        || (mode == 1 && (b->coupled || !b->tc_ok))) {
         return VFPS_ERR_INVALID_ARGUMENT;
     }
     return bguard(b->ctx, [&] {

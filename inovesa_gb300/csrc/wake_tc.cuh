@@ -11,13 +11,18 @@
 // memory.  The dropped T_lo P_lo term and the TF32 rounding of the lo
 // parts are below 2^-20 of each product: FP32-level accuracy.
 //
-// One CTA (4 warps) per tile of 128 mesh rows x 64 bunches; K in chunks of
-// 32 (128 bytes of TF32 per row) staged in shared memory in the 128-byte
-// swizzled K-major layout (8-row atoms of 1024 bytes; the 16-byte chunk c
-// of row r sits at chunk c ^ (r & 7)); one thread issues the MMAs and
-// commits them to an mbarrier that every thread waits on (bounded) before
-// the chunk is overwritten.  The accumulator (128 lanes x 64 columns of
-// FP32) is read back with tcgen05.ld, one 32-lane slice per warp.
+// One CTA (4 warps) per tile of 128 mesh rows x 16 bunches, K in chunks of
+// 32 (128 bytes of TF32 per row).  The T operand is constant: the host
+// stores each (row tile, chunk) as the byte image of its shared-memory
+// tile (hi plane, then lo plane, 128-byte swizzled K-major: 8-row atoms of
+// 1024 bytes, the 16-byte chunk c of row r at chunk c ^ (r & 7)), so one
+// bulk copy of 32 KiB stages a chunk, up to six chunks in flight.  The
+// profiles (the B operand) are split into hi and lo and swizzled by the
+// CTA's threads, all chunks at once.  One thread issues the MMAs of a chunk
+// as it lands and commits them to that stage's mbarrier, which frees the
+// stage for the chunk as many stages further on; every wait is bounded.  The
+// accumulator (128 lanes x 16 columns of FP32) is read back with
+// tcgen05.ld, one 32-lane slice per warp.
 #pragma once
 
 #include <cstring>
@@ -27,21 +32,45 @@
 namespace {
 
 constexpr int TC_M = 128;         // mesh rows per tile (TMEM lanes)
-constexpr int TC_N = 64;          // bunches per tile (TMEM columns)
-constexpr int TC_K = 32;          // K of one staged chunk (128 bytes)
+constexpr int TC_N = 16;          // bunches per tile (TMEM columns)
+constexpr int TC_K = 32;          // K of one chunk (128 bytes)
 constexpr int TC_THREADS = 128;
+constexpr int TC_MAX_STAGES = 6;  // T chunks in flight, at most
+constexpr int TC_MAX_N = 1024;    // widest mesh (shared memory of B)
+constexpr uint32_t TC_TMEM_COLS = 32;              // smallest allocation
 constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 4;   // 16 KiB per plane
-constexpr uint32_t TC_B_BYTES = TC_N * TC_K * 4;   //  8 KiB per plane
-// A_hi, A_lo, B_hi, B_lo (1024-byte aligned), then the barrier, the TMEM
-// address and the tile's bunch table; +1024 to align the dynamic base
-constexpr uint32_t TC_SMEM = 1024 + 2 * TC_A_BYTES + 2 * TC_B_BYTES + 1024;
+constexpr uint32_t TC_B_BYTES = TC_N * TC_K * 4;   //  2 KiB per plane
+constexpr uint32_t TC_IMG_FLOATS = TC_M * TC_K;    // floats of one plane
+
+constexpr uint32_t TC_SMEM_MAX = 232448;          // per CTA (227 KiB)
+
+// T chunks in flight for an n-row mesh: as many stages as fit next to all
+// of B (at most TC_MAX_STAGES, at most the number of chunks)
+__host__ __device__ constexpr int tc_stages(int n)
+{
+    const int nkc = n / TC_K;
+    const int room = int((TC_SMEM_MAX - 1536 - uint32_t(nkc) * 2 * TC_B_BYTES)
+                         / (2 * TC_A_BYTES));
+    const int s = room < TC_MAX_STAGES ? room : TC_MAX_STAGES;
+    return s < nkc ? s : nkc;
+}
+
+// dynamic shared memory of an n-row mesh: +1024 to align the base, the T
+// stages (hi, lo), every B chunk (hi, lo), barriers and the tile's bunch
+// table
+__host__ __device__ constexpr uint32_t tc_smem(int n)
+{
+    return 1024 + uint32_t(tc_stages(n)) * 2 * TC_A_BYTES
+           + uint32_t(n / TC_K) * 2 * TC_B_BYTES + 512;
+}
 
 // one tile of bunches sharing n and the impedance
 struct TcGroup {
-    uint32_t n;          // mesh size
-    uint32_t t_off;      // T_hi at t_off, T_lo at t_off + n * n
+    uint32_t n;          // mesh size (a multiple of TC_K, at most TC_MAX_N)
+    uint32_t t_off;      // the T images: [row tile][chunk][hi, lo plane]
     uint32_t nbt;        // bunches in this tile (<= TC_N)
-    uint32_t list_off;   // their indices: list[list_off .. + nbt)
+    uint32_t list_off;   // their profile offsets and wake scalings (bits):
+                         // list[list_off .. + nbt)
 };
 
 __host__ __device__ inline float tf32_hi(float v)
@@ -131,102 +160,134 @@ __device__ __forceinline__ void sw128_store(uint8_t* tile, int r, int c,
 }
 
 __global__ void __launch_bounds__(TC_THREADS)
-k_wake_tc(const BDev* __restrict__ bd, const TcGroup* __restrict__ groups,
-          const uint32_t* __restrict__ list,
+k_wake_tc(const TcGroup* __restrict__ groups,
+          const uint2* __restrict__ list,
           const float* __restrict__ tplanes, const float* __restrict__ pin,
           float* __restrict__ wake, int* __restrict__ status)
 {
     extern __shared__ uint8_t tc_raw[];
     const TcGroup G = groups[blockIdx.y];
     const int n = int(G.n);
-    const int x0 = int(blockIdx.x) * TC_M;
+    const int mt = int(blockIdx.x);
+    const int x0 = mt * TC_M;
     if (x0 >= n) {
         return;    // the whole CTA, before any barrier or allocation
     }
+    const int nkc = n / TC_K;
+    const int stages = tc_stages(n);
     uint8_t* base = reinterpret_cast<uint8_t*>(
         (reinterpret_cast<uintptr_t>(tc_raw) + 1023) & ~uintptr_t(1023));
-    uint8_t* a_hi = base;
-    uint8_t* a_lo = a_hi + TC_A_BYTES;
-    uint8_t* b_hi = a_lo + TC_A_BYTES;
-    uint8_t* b_lo = b_hi + TC_B_BYTES;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(b_lo + TC_B_BYTES);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar + 1);
+    uint8_t* a_st = base;                                  // [stage][hi, lo]
+    uint8_t* b_ch = a_st + stages * 2 * TC_A_BYTES;        // [chunk][hi, lo]
+    uint64_t* full = reinterpret_cast<uint64_t*>(b_ch
+                                                 + nkc * 2 * TC_B_BYTES);
+    uint64_t* empty = full + TC_MAX_STAGES;
+    uint64_t* done = empty + TC_MAX_STAGES;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(done + 1);
     uint32_t* poff = tmem_slot + 4;                  // [TC_N]
     float* scale = reinterpret_cast<float*>(poff + TC_N);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int nbt = int(G.nbt);
+    // this row tile's T images: chunk kc at img + kc * 2 planes
+    const float* img = tplanes + G.t_off
+                       + size_t(mt) * nkc * 2 * TC_IMG_FLOATS;
 
     if (tid < TC_N) {
         if (tid < nbt) {
-            const BDev B = bd[list[G.list_off + tid]];
-            poff[tid] = B.prof_off;
-            scale[tid] = B.wakescale;
+            const uint2 e = list[G.list_off + tid];
+            poff[tid] = e.x;
+            scale[tid] = __uint_as_float(e.y);
         } else {
             poff[tid] = 0;
             scale[tid] = 0.f;
         }
     }
+    int issued[TC_MAX_STAGES] = {};     // thread 0: loads per stage
     if (tid == 0) {
-        mbar_init(bar, 1);
+        for (int s = 0; s < stages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
         mbar_fence_init();
+        // the first chunks of T while the profiles are split
+        for (int s = 0; s < stages; s++) {
+            mbar_arrive_expect_tx(&full[s], 2 * TC_A_BYTES);
+            tma_load_1d(a_st + s * 2 * TC_A_BYTES,
+                        img + size_t(s) * 2 * TC_IMG_FLOATS, 2 * TC_A_BYTES,
+                        &full[s]);
+            issued[s]++;
+        }
     }
     if (warp == 0) {
         asm volatile(
             "tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
-            :: "r"(smem_addr(tmem_slot)), "r"(uint32_t(TC_N)) : "memory");
+            :: "r"(smem_addr(tmem_slot)), "r"(TC_TMEM_COLS) : "memory");
         asm volatile(
             "tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;"
             ::: "memory");
     }
+    __syncthreads();   // poff for the profile loads below
+    // B: every chunk of the tile's profiles, split into hi and lo; 8
+    // loads per thread in flight at a time
+    {
+        const int q4 = n >> 2;                 // float4 per profile
+        const int total = TC_N * q4;
+        for (int i0 = 0; i0 < total; i0 += 8 * TC_THREADS) {
+            float4 v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * TC_THREADS + tid;
+                const int j = i / q4, q = i - j * q4;
+                v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (i < total && j < nbt) {
+                    v[u] = *reinterpret_cast<const float4*>(pin + poff[j]
+                                                            + 4 * q);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * TC_THREADS + tid;
+                if (i < total) {
+                    const int j = i / q4, q = i - j * q4;
+                    const int kc = q >> 3, c = q & 7;
+                    const float4 h = make_float4(
+                        tf32_hi(v[u].x), tf32_hi(v[u].y), tf32_hi(v[u].z),
+                        tf32_hi(v[u].w));
+                    const float4 l = make_float4(
+                        v[u].x - h.x, v[u].y - h.y, v[u].z - h.z,
+                        v[u].w - h.w);
+                    uint8_t* t = b_ch + kc * 2 * TC_B_BYTES;
+                    sw128_store(t, j, c, h);
+                    sw128_store(t + TC_B_BYTES, j, c, l);
+                }
+            }
+        }
+    }
+    // the tensor cores read shared memory through the async proxy
+    fence_proxy_async();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<volatile uint32_t*>(tmem_slot);
 
-    const float* t_hi = tplanes + G.t_off;
-    const float* t_lo = t_hi + size_t(n) * n;
-    const uint32_t idesc = idesc_tf32(TC_M, TC_N);
-    const int nchunks = n / TC_K;
-    bool ok = true;
-    for (int kc = 0; kc < nchunks && ok; kc++) {
-        const int m0 = kc * TC_K;
-        // A: 128 rows x 8 chunks of 16 bytes, hi and lo planes
-        for (int i = tid; i < TC_M * 8; i += TC_THREADS) {
-            const int r = i >> 3, c = i & 7;
-            const int x = x0 + r;
-            float4 h = make_float4(0.f, 0.f, 0.f, 0.f), l = h;
-            if (x < n) {
-                h = *reinterpret_cast<const float4*>(
-                    t_hi + size_t(x) * n + m0 + 4 * c);
-                l = *reinterpret_cast<const float4*>(
-                    t_lo + size_t(x) * n + m0 + 4 * c);
+    bool ok = true;    // thread 0: every chunk arrived in time
+    if (tid == 0) {
+        const uint32_t idesc = idesc_tf32(TC_M, TC_N);
+        int consumed[TC_MAX_STAGES] = {};
+        for (int kc = 0; kc < nkc; kc++) {
+            const int s = kc % stages;
+            if (!mbar_wait_bounded(&full[s], uint32_t(consumed[s] & 1),
+                                   WAIT_NS)) {
+                ok = false;
+                break;
             }
-            sw128_store(a_hi, r, c, h);
-            sw128_store(a_lo, r, c, l);
-        }
-        // B: 64 bunch rows x 8 chunks, split into hi and lo here
-        for (int i = tid; i < TC_N * 8; i += TC_THREADS) {
-            const int j = i >> 3, c = i & 7;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (j < nbt) {
-                v = *reinterpret_cast<const float4*>(pin + poff[j] + m0
-                                                     + 4 * c);
-            }
-            const float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y),
-                                         tf32_hi(v.z), tf32_hi(v.w));
-            const float4 l = make_float4(v.x - h.x, v.y - h.y, v.z - h.z,
-                                         v.w - h.w);
-            sw128_store(b_hi, j, c, h);
-            sw128_store(b_lo, j, c, l);
-        }
-        // the tensor cores read shared memory through the async proxy
-        fence_proxy_async();
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-        if (tid == 0) {
-            const uint32_t sa_hi = smem_addr(a_hi), sa_lo = smem_addr(a_lo);
-            const uint32_t sb_hi = smem_addr(b_hi), sb_lo = smem_addr(b_lo);
+            consumed[s]++;
+            tc_fence_after();
+            const uint32_t sa_hi = smem_addr(a_st + s * 2 * TC_A_BYTES);
+            const uint32_t sa_lo = sa_hi + TC_A_BYTES;
+            const uint32_t sb_hi = smem_addr(b_ch + kc * 2 * TC_B_BYTES);
+            const uint32_t sb_lo = sb_hi + TC_B_BYTES;
 #pragma unroll
             for (int kk = 0; kk < TC_K / 8; kk++) {
                 // 8 TF32 of K = 32 bytes further into each 128-byte row
@@ -239,32 +300,56 @@ k_wake_tc(const BDev* __restrict__ bd, const TcGroup* __restrict__ groups,
                 tc_mma_tf32(tmem, sdesc_sw128(sa_lo + o),
                             sdesc_sw128(sb_hi + o), idesc, 1u);
             }
-            tc_commit(bar);
+            tc_commit(&empty[s]);
+            // the previous chunk's stage takes the chunk `stages` after it
+            // once its products are done
+            const int kp = kc - 1;
+            if (kp >= 0 && kp + stages < nkc) {
+                const int sp = kp % stages;
+                if (!mbar_wait_bounded(&empty[sp],
+                                       uint32_t((kp / stages) & 1),
+                                       WAIT_NS)) {
+                    ok = false;
+                    break;
+                }
+                mbar_arrive_expect_tx(&full[sp], 2 * TC_A_BYTES);
+                tma_load_1d(a_st + sp * 2 * TC_A_BYTES,
+                            img + size_t(kp + stages) * 2 * TC_IMG_FLOATS,
+                            2 * TC_A_BYTES, &full[sp]);
+                issued[sp]++;
+            }
         }
-        // all MMAs of this chunk done before its operands are overwritten
-        bool done = mbar_wait_bounded(bar, uint32_t(kc & 1), WAIT_NS);
-        if (!done) {
+        // every product issued so far completes before done arrives
+        tc_commit(done);
+        if (!ok) {
             atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
-            mbar_wait_bounded(bar, uint32_t(kc & 1), WAIT_NS);
+            // the copies still in flight land before the CTA ends
+            for (int s = 0; s < stages; s++) {
+                while (consumed[s] < issued[s]) {
+                    mbar_wait_bounded(&full[s], uint32_t(consumed[s] & 1),
+                                      WAIT_NS);
+                    consumed[s]++;
+                }
+            }
         }
-        ok = __syncthreads_and(done) != 0;   // the same for every thread
     }
+    bool fin = mbar_wait_bounded(done, 0u, WAIT_NS);
+    if (!fin && tid == 0) {
+        atomicCAS(status, 0, VFPS_ERR_TIMEOUT);
+    }
+    const bool all = __syncthreads_and(fin && ok) != 0;
     tc_fence_after();
-    if (ok) {
+    if (all) {
         // warp w reads lanes 32w..32w+31 (rows x0 + 32w + lane)
         const int x = x0 + 32 * warp + lane;
         const uint32_t ta = tmem + (uint32_t(32 * warp) << 16);
+        float v[16];
+        tc_ld16(ta, v);
+        if (x < n) {
 #pragma unroll
-        for (int c0 = 0; c0 < TC_N; c0 += 16) {
-            float v[16];
-            tc_ld16(ta + uint32_t(c0), v);
-            if (x < n) {
-#pragma unroll
-                for (int j = 0; j < 16; j++) {
-                    if (c0 + j < nbt) {
-                        wake[poff[c0 + j] + x] = __fmul_rn(scale[c0 + j],
-                                                           v[j]);
-                    }
+            for (int j = 0; j < 16; j++) {
+                if (j < nbt) {
+                    wake[poff[j] + x] = __fmul_rn(scale[j], v[j]);
                 }
             }
         }
@@ -273,7 +358,7 @@ k_wake_tc(const BDev* __restrict__ bd, const TcGroup* __restrict__ groups,
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;"
-                     :: "r"(tmem), "r"(uint32_t(TC_N)) : "memory");
+                     :: "r"(tmem), "r"(TC_TMEM_COLS) : "memory");
     }
 }
 
