@@ -678,6 +678,7 @@ void upload_offset(vfps_map* m, const std::vector<float>& off)
     VFPS_REQUIRE(off.size() == m->offset.n, "offset has the wrong length");
     m->host_offset = off;
     m->host_offset_valid = true;
+    m->xtab_valid = false;
     h2d(m->offset.p, off.data(), off.size(), m->in->ctx);
 }
 

@@ -226,13 +226,33 @@ __global__ void k_kick_y4(const float* __restrict__ in,
     }
 }
 
+// the x-kick's stencils of every column, tap-major: shift[j][y], w[j][y]
+// (the same function the kernels evaluate, computed once per set of
+// offsets)
+__global__ void k_kick_table(const float* __restrict__ offsets, uint32_t n,
+                             int it, int* __restrict__ shift,
+                             float* __restrict__ w)
+{
+    const uint32_t y = blockIdx.x * blockDim.x + threadIdx.x;
+    if (y >= n) {
+        return;
+    }
+    const KickStencil s = kick_stencil(offsets[y], n, it);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        shift[j * n + y] = s.shift[j];
+        w[j * n + y] = s.w[j];
+    }
+}
+
 // x-kick: a CTA per block of rows of one bunch; each thread owns 4
-// columns (their stencils, one per column, in registers for the block)
-// and sweeps the rows with 16-byte reads where the 4 columns take the
-// same shifts, column by column otherwise
+// columns (their stencils, one per column, loaded from the table in
+// 16-byte words) and sweeps the rows with 16-byte reads where the 4
+// columns take the same shifts, column by column otherwise
 __global__ void k_kick_x4(const float* __restrict__ in,
                           float* __restrict__ out,
-                          const float* __restrict__ offsets, uint32_t n,
+                          const int* __restrict__ shtab,
+                          const float* __restrict__ wtab, uint32_t n,
                           int it, int rows)
 {
     const int n4 = int(n / 4);
@@ -244,8 +264,19 @@ __global__ void k_kick_x4(const float* __restrict__ in,
     for (int g = threadIdx.x; g < n4; g += blockDim.x) {
         KickStencil s[4];
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            s[c] = kick_stencil(offsets[4 * g + c], n, it);
+        for (int j = 0; j < 4; j++) {
+            const int4 sh = __ldg(reinterpret_cast<const int4*>(
+                                      shtab + size_t(j) * n) + g);
+            const float4 wv = __ldg(reinterpret_cast<const float4*>(
+                                        wtab + size_t(j) * n) + g);
+            s[0].shift[j] = sh.x;
+            s[1].shift[j] = sh.y;
+            s[2].shift[j] = sh.z;
+            s[3].shift[j] = sh.w;
+            s[0].w[j] = wv.x;
+            s[1].w[j] = wv.y;
+            s[2].w[j] = wv.z;
+            s[3].w[j] = wv.w;
         }
         bool same = true;
 #pragma unroll
@@ -473,10 +504,19 @@ void launch_kick(const vfps_map* m, const float* offset)
         k_kick_y4<<<in->nb * n, t4, smem, in->ctx->stream>>>(
             in->data.p, m->out->data.p, offset, n, m->it);
     } else if (v4) {
+        if (!m->xtab_valid) {
+            m->xshift.alloc(size_t(4) * n);
+            m->xweight.alloc(size_t(4) * n);
+            k_kick_table<<<(n + 127) / 128, 128, 0, in->ctx->stream>>>(
+                offset, n, m->it, m->xshift.p, m->xweight.p);
+            VFPS_LAUNCHED();
+            m->xtab_valid = true;
+        }
         const int rows = plain_rows(n, in->nb);
         dim3 grid((n + rows - 1) / rows, in->nb);
         k_kick_x4<<<grid, t4, 0, in->ctx->stream>>>(
-            in->data.p, m->out->data.p, offset, n, m->it, rows);
+            in->data.p, m->out->data.p, m->xshift.p, m->xweight.p, n, m->it,
+            rows);
     } else if (m->axis == VFPS_AXIS_Y) {
         const int threads = n >= 256 ? 256 : ((n + 31) / 32) * 32;
         k_kick_y<<<in->nb * n, threads, 0, in->ctx->stream>>>(

@@ -197,6 +197,11 @@ struct vfps_map {
     vfps_field* field = nullptr;
     std::vector<float> host_offset;  // mirror for applyTo / getForce
     bool host_offset_valid = true;
+    // x-kick: the stencils of the current offsets, tap-major [4][n] (the
+    // row-sweep kernel reads them instead of evaluating them per row)
+    mutable vfps::DevBuf<int> xshift;
+    mutable vfps::DevBuf<float> xweight;
+    mutable bool xtab_valid = false;
     // DynamicRFKickMap: per-step phase and amplitude drawn on the device
     bool dynrf = false;
     DynRf dyn;
