@@ -190,7 +190,7 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
     RowInfo7* S = reinterpret_cast<RowInfo7*>(base + L.s);
     float* T = reinterpret_cast<float*>(base + L.tab);
     uint64_t* bar = reinterpret_cast<uint64_t*>(base + L.bar);
-    // 512 rows: the halves' row sums of a tile, [2 tiles][2 halves][rb/2]
+    // 512, 1024 rows: the parts' row sums of a tile, [2 tiles][PARTS][rb/2]
     float* part = reinterpret_cast<float*>(base + L.part);
     const int rb = int(L.rb);
     constexpr int rs = N + 2 * APAD + 16;   // astride0(N), the ring's L.rs
