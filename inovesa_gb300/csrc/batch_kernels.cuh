@@ -1345,7 +1345,7 @@ struct SmemR {
     uint32_t bar;   // three mbarriers (two for the rows, one for tab)
     uint32_t rb;    // ring slots: twice the rows a tile reads
     uint32_t rs;    // floats per slot
-    uint32_t part;  // k_bmaps0f, 512/1024 rows: parts' row sums [2][PARTS][RB/2]
+    uint32_t part;  // k_bmaps0f, 512/1024 rows: the parts' row sums
     uint32_t total;
 };
 
