@@ -4,9 +4,11 @@ state, against the FP64 wake of the same profiles, and through a solver run
 against the FP64 oracle.
 
 Tolerances: the error against the FP64 product of the same profiles, per
-bunch relative to its largest wake value, is at most 2e-5 and within 4x of
-the CUDA-core FP32 sum's (the Toeplitz sum cancels: its terms are up to
-ten times the result); solver densities, relative L1 <= 1e-4.
+bunch relative to its largest wake value, is at most 2.5e-5 for meshes up
+to 256 rows (growing as the square root of the mesh size beyond: FP32
+accumulation over n source cells) and within 4x of the CUDA-core FP32
+sum's (the Toeplitz sum cancels: its terms are up to ten times the
+result); solver densities, relative L1 <= 1e-4.
 """
 import numpy as np
 import pytest
@@ -44,11 +46,17 @@ def scan_batch(ctx, counts):
     return b, specs, zdata
 
 
-def test_wake_tc_matches_cuda_cores_and_fp64(gpu_ctx):
-    # 70 bunches of 256 rows (two tiles: 64 + 6) and 3 of 128; two
-    # identical batches reach the same state, then one step each with the
-    # wake on the CUDA cores and on the tensor cores
-    counts = {256: 70, 128: 3}
+# 70 bunches of 256 rows (five tiles of 16, the last with 6) and 3 of
+# 128; 1024-row meshes (three chunks of the Toeplitz operand in flight,
+# all 32 profile chunks staged) next to 64-row ones (two chunks, fewer than
+# the stages); 512 rows (five in flight)
+WAKE_TC_MIXES = [{256: 70, 128: 3}, {1024: 5, 64: 17}, {512: 20}]
+
+
+@pytest.mark.parametrize("counts", WAKE_TC_MIXES)
+def test_wake_tc_matches_cuda_cores_and_fp64(gpu_ctx, counts):
+    # two identical batches reach the same state, then one step each with
+    # the wake on the CUDA cores and on the tensor cores
     b0, specs, zdata = scan_batch(gpu_ctx, counts)
     b1, _, _ = scan_batch(gpu_ctx, counts)
     b0.step(30)
@@ -73,7 +81,9 @@ def test_wake_tc_matches_cuda_cores_and_fp64(gpu_ctx):
         e_tc = max(e_tc, np.abs(w1[off:off + n] - ref).max() / m)
     print("wake error vs FP64 (max over bunches, relative to max |wake|):"
           " CUDA cores %.2e, tensor cores %.2e" % (e_cc, e_tc))
-    assert e_tc <= 2e-5, e_tc
+    # FP32 accumulation over K = n source cells: the bound grows as sqrt(n)
+    bound = 2.5e-5 * max(1.0, np.sqrt(max(counts) / 256.0))
+    assert e_tc <= bound, (e_tc, bound)
     assert e_tc <= 4 * e_cc + 1e-6, (e_tc, e_cc)
 
 
