@@ -112,3 +112,27 @@ def test_side_not_multiple_of_4(gpu_ctx, monkeypatch):
     idx, w = oracle.fp_stencils(n, AXES, e1, 3, 4, dtype=np.float32)
     ref = oracle.fp_apply(d, 4, idx, w, dtype=np.float32)
     assert np.max(np.abs(b.getData() - ref)) <= 2e-6 * np.abs(ref).max()
+
+
+def test_x_kick_new_offsets(gpu_ctx, monkeypatch):
+    """An x-kick map applied, given new offsets and applied again computes
+    with the new ones (its stencil table is rebuilt): equal to a fresh map
+    with those offsets, bit for bit."""
+    use_cells(monkeypatch, False)
+    n = 128
+    d = density(n, 2, seed=5)
+    a, b = pair(gpu_ctx, n, d)
+    km = V.KickMap(a, b, 4, False, 0)
+    count = km.getForce().size
+    km.swapOffset(kick_offsets(n, count, seed=1))
+    km.apply()
+    off2 = kick_offsets(n, count, seed=2)
+    km.swapOffset(off2)
+    km.apply()
+    again = b.getData()
+    a2, b2 = pair(gpu_ctx, n, d)
+    fresh = V.KickMap(a2, b2, 4, False, 0)
+    fresh.swapOffset(off2)
+    fresh.apply()
+    np.testing.assert_array_equal(again, b2.getData())
+    assert gpu_ctx.device_status() == 0
