@@ -368,6 +368,12 @@ k_bwake(const BDev* __restrict__ bd, const uint2* __restrict__ wblk,
     if (B.chain == 0 && x0 < R) {
         sb0 = rf[xr0 + x0];
     }
+    // the profile's lines into L2 ahead of their loads after the wait (a
+    // hint: the previous maps kernel's writes still land in L2 after it,
+    // so the loads read them either way)
+    for (int i = 32 * threadIdx.x; i < n; i += 32 * THREADS) {
+        prefetch_l2(pin + B.prof_off + i);
+    }
     // the records and tables above do not change between steps; launched
     // as a programmatic dependent of the previous step's maps kernel, the
     // CTA reads them while that kernel ends, and waits for it here before
