@@ -158,6 +158,37 @@ __device__ __forceinline__ float4 fp4(const float (&w)[7], const float4& f0,
     return make_float4(o[0], o[1], o[2], o[3]);
 }
 
+// issue_rows with the row copies spread over the CTA's warps (row i of the
+// new rows from lane i / warps of warp i % warps), so that no warp issues
+// them all.  A copy may complete before thread 0 has set the expected
+// bytes: the barrier's phase still waits for that thread's arrival
+template <int NT>
+__device__ __forceinline__ void issue_rows_cta(const BDev& B, int lo, int hi,
+                                               const RingMap& m, float* ring,
+                                               int rb, int rs,
+                                               const float* __restrict__ din,
+                                               const RowInfo7* __restrict__ rinfo,
+                                               RowInfo7* S, uint64_t* bar)
+{
+    const int n = int(B.n);
+    const int a = max(lo, 0), e = max(min(hi, n), a);
+    const uint32_t row_bytes = uint32_t(n) * 4u;
+    const uint32_t ri_bytes = uint32_t(e - a) * uint32_t(sizeof(RowInfo7));
+    if (threadIdx.x == 0) {
+        fence_proxy_async();
+        mbar_arrive_expect_tx(bar, uint32_t(e - a) * row_bytes + ri_bytes);
+        if (e > a) {
+            tma_load_1d(S + (a - lo), rinfo + B.prof_off + a, ri_bytes, bar);
+        }
+    }
+    constexpr int NW = NT / 32;
+    const int i = (threadIdx.x >> 5) + NW * (threadIdx.x & 31);
+    for (int x = a + i; x < e; x += NT) {
+        tma_load_1d(ring + size_t(m.slot(x, rb)) * rs + APAD,
+                    din + B.dens_off + size_t(x) * n, row_bytes, bar);
+    }
+}
+
 // meshes of 512 and 1024 rows: rows in parts of 256 columns, one warp each
 // in stage 2; 1024-row lattices take a 5-row drift window (groups of 4
 // columns may span two drift shifts) and an 11-plane table
@@ -388,10 +419,8 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 mn = RingMap::at(xr, front);
             }
             front = mn.slot(hi_n, rb);
-            if (threadIdx.x < 32) {
-                issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo, S,
-                           &bar[(k + 1) & 1]);
-            }
+            issue_rows_cta<NT>(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo,
+                               S, &bar[(k + 1) & 1]);
         }
 
         // this tile's drift and Fokker-Planck planes in T
