@@ -419,8 +419,17 @@ k_bmaps0f(const BDev* __restrict__ bd, const Tile* __restrict__ tiles,
                 mn = RingMap::at(xr, front);
             }
             front = mn.slot(hi_n, rb);
-            issue_rows_cta<NT>(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo,
+            // (spread over the warps where a row is one warp's; the parts of
+            // 512 and 1024 rows were measured faster with warp 0 alone)
+            if constexpr (HALF) {
+                if (threadIdx.x < 32) {
+                    issue_rows(Bn, lo_n, hi_n, mn, ring, rb, rs, din, rinfo,
                                S, &bar[(k + 1) & 1]);
+                }
+            } else {
+                issue_rows_cta<NT>(Bn, lo_n, hi_n, mn, ring, rb, rs, din,
+                                   rinfo, S, &bar[(k + 1) & 1]);
+            }
         }
 
         // this tile's drift and Fokker-Planck planes in T
