@@ -1,8 +1,8 @@
 /* C++ façade over the C ABI of vfps.h with the reference's class names and
  * constructor parameters, so that a solver loop written against
- * inc/PS/PhaseSpace.hpp, inc/SM/*.hpp, inc/PS/ElectricField.hpp and
- * inc/Z/*.hpp compiles against the GPU path with the handle type
- * (vfps::ctxptr_t instead of oclhptr_t) as the only change.
+ * inc/PS/PhaseSpace.hpp, the map headers of inc/SM, inc/PS/ElectricField.hpp
+ * and the impedance headers of inc/Z compiles against the GPU path with the
+ * handle type (vfps::ctxptr_t instead of oclhptr_t) as the only change.
  *
  * Header only; link with libvfps.so.  Errors become exceptions as in the
  * reference: std::invalid_argument for VFPS_ERR_INVALID_ARGUMENT (bad
