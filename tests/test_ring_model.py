@@ -10,7 +10,9 @@ on, for mixes of mesh sizes, halos and tile sizes:
 * the slot arithmetic's precondition: 0 <= x - xref + pref < 2 rb, so one
   conditional subtraction reduces it;
 * the byte count of a tile's bulk copies is never negative (a short last
-  tile whose new rows all lie beyond the mesh stages none).
+  tile whose new rows all lie beyond the mesh stages none);
+* the fast kernel's row copies, spread over its warps, copy every new row
+  of a tile exactly once.
 
 No GPU: the model restates the kernels' index arithmetic in Python."""
 import itertools
@@ -197,3 +199,24 @@ def test_model_detects_a_small_ring():
     with pytest.raises(AssertionError):
         for c in range(3):
             walk(bunches, tiles, rb - 1, c, 3)
+
+
+@pytest.mark.parametrize("nt", [128, 256])
+def test_row_copies_spread_over_warps(nt):
+    """issue_rows_cta (ring_fast.cuh): thread t issues rows a + i,
+    a + i + NT, ... with i = t / 32 + (NT / 32) (t % 32); every new row of
+    a tile is copied exactly once, for every count of new rows, and the
+    rows of a tile of at most 32 land on a few lanes of each warp."""
+    nw = nt // 32
+    for m in range(0, 3 * nt + 5):
+        seen = []
+        lanes_per_warp = [0] * nw
+        for t in range(nt):
+            i = t // 32 + nw * (t % 32)
+            rows = list(range(i, m, nt))
+            seen.extend(rows)
+            if rows:
+                lanes_per_warp[t // 32] += 1
+        assert sorted(seen) == list(range(m)), m
+        if m <= 32:
+            assert max(lanes_per_warp) - min(lanes_per_warp) <= 1, m
